@@ -1,0 +1,333 @@
+#!/usr/bin/env python
+"""Benchmark: the fused star query on one GB300 (or N, one rank per GPU).
+
+Default workload (N=1): the 600 M-row four-dimension star schema, query
+"date + customer + supplier join, GROUP BY (c_nation, s_nation, year)
+SUM(revenue - supplycost)", fact columns resident in HBM.  A step is one
+RunPipelineCMD of that fact pipeline (scan + probes + aggregate + result
+materialisation); the dimension pipelines and their tables are built during
+warm-up and stay cached, as in the served form.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--config 0|1|2]
+
+Under torchrun each rank owns its own slice of one global fact table (rows
+rank*R .. rank*R+R-1), so per-GPU work is fixed ("weak" scaling); ranks only
+meet at the timing barriers.  The reference arm (--impl reference) times the
+reference's generated CPU path (the oracle port: codegen.py text compiled with
+g++ -O2, run bulk by bulk on every host core) on a bounded sample of the same
+workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "fact rows/s"
+UNIT = "rows/s"
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def measured_hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic(config: int):
+    """DRAM bytes per fact row of the star kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "star_kernel_traffic.json")
+    try:
+        d = json.load(open(p))
+        return d[f"config{config}"]
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (clocks and throttle reasons)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names[1:], f[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference_run(cfg: int, sample_rows: int, steps: int, threads: int):
+    """The reference's generated CPU path (oracle port) on `sample_rows` fact rows.
+    Returns (rows/s per step list, hash build ms, description)."""
+    import oracle
+    from shadowvm_gb300 import workloads as W
+    w = W.make(cfg, fact_rows=sample_rows)
+    used = {0: [0, 1, 2, 3], 1: [0, 4, 5], 2: [0, 5, 6, 7, 8]}[cfg]
+    fact = []
+    from shadowvm_gb300 import datagen as dg
+    # generate only the columns the query reads; the others stay zero
+    for c, name in enumerate(w.fact_cols):
+        if c in used:
+            fact.append(dg.fact_column(name, 0, sample_rows, seed=w.seed, n_part=w.n_part, n_cust=w.n_cust,
+                                       n_supp=w.n_supp, datekeys=w.dims["date"][0]))
+        else:
+            fact.append(np.zeros(sample_rows, np.int32))
+    rates, opens = [], []
+    for _ in range(steps):
+        _, stats = oracle.run_workload(w, "port", threads=threads, fact=fact)
+        rates.append(sample_rows / (stats.compute_ms / 1e3))
+        opens.append(stats.open_ms)
+    desc = (f"{sample_rows} fact rows (rows 0..{sample_rows - 1}) of config {cfg}, tuple_per_bulk "
+            f"{w.tuple_per_bulk}, generated host loop compiled by g++ -O2 (key bytes hashed as signed char), "
+            f"{threads} worker threads; pipeline compute time (transform + reduce), hash build excluded "
+            f"({statistics.median(opens):.0f} ms)")
+    return rates, statistics.median(opens), desc
+
+
+def default_cpu_sample(cfg: int, threads: int) -> int:
+    """One reference bulk per host thread (the reference runs one task per bulk,
+    core/pipeline.cu:161-212), at most 32 bulks."""
+    tpb = 3_000_000 if cfg == 2 else 2_000_000
+    return tpb * max(4, min(threads, 32))
+
+
+def reference_arm(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sample = args.cpu_sample_rows or default_cpu_sample(args.config, threads)
+    _ = cpu_reference_run(args.config, min(sample, 3_000_000), 1, threads)  # compile + warm caches
+    for _ in range(max(0, args.warmup - 1)):
+        cpu_reference_run(args.config, sample, 1, threads)
+    t0 = time.time()
+    rates, _, desc = cpu_reference_run(args.config, sample, args.steps, threads)
+    wall = time.time() - t0
+    v = statistics.median(rates)
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": sample / v * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+           "data": "synthetic (seeded counter-based generator, star-schema shapes)",
+           "config": workload_config(args.config, sample),
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "wall_s": wall}
+    print(json.dumps(out))
+
+
+def workload_config(cfg: int, rows: int):
+    names = {0: "date join, SUM(extprice*discount)", 1: "date+part join, GROUP BY (year, brand) SUM(revenue)",
+             2: "4-dimension star schema: date+customer+supplier join, GROUP BY (c_nation, s_nation, year) "
+                "SUM(revenue-supplycost)"}
+    return {"workload": f"config {cfg}: {names[cfg]}", "fact_rows": rows,
+            "fact_columns_read": {0: 4, 1: 3, 2: 5}[cfg], "int32_columns": True,
+            "l2": "inputs larger than L2 (no flush needed)" if rows * 4 > 129e6 else "flush not applied"}
+
+
+def ours_arm(args):
+    import torch
+    from shadowvm_gb300 import Engine, capi
+    from shadowvm_gb300 import workloads as W
+
+    rank, world, local = rank_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    w = W.make(args.config, fact_rows=args.rows)
+    rows = w.fact_rows
+    eng = Engine(device=local, tuple_per_bulk=w.tuple_per_bulk, join_mode=args.join_mode)
+    W.load_engine(eng, w, row0=rank * rows)
+    t_build0 = time.time()
+    for p in w.dim_pipelines:
+        eng.run(p)
+    eng.run(w.query)  # builds and caches the dimension tables
+    build_s = time.time() - t_build0
+    stream = torch.cuda.ExternalStream(eng.stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        eng.run(w.query)
+    clocks = ClockSampler(local)
+    clocks.start()
+    eng.profile(True)
+    eng.profile_reset()
+    barrier()
+    l0 = eng.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        eng.run(w.query)
+    e1.record(stream)
+    barrier()
+    launches = eng.kernel_launches() - l0
+    ms = e0.elapsed_time(e1)
+    n_star, star_ms = eng.profile_read(capi.K_STAR)
+    eng.profile(False)
+    clk = clocks.stop()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = rows * world / (ms_step / 1e3)
+
+    # roofline of the star kernel (algorithmic bytes / event-timed launch duration)
+    bpr = w.fact_bytes_per_row()
+    star_avg_s = (star_ms / max(n_star, 1)) / 1e3
+    achieved = rows * bpr / star_avg_s / 1e9
+    peak, peak_src = measured_hbm_peak()
+    tr = committed_traffic(args.config)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": (tr["dram_bytes_per_row"] * rows) if tr else None,
+                "algorithmic_bytes_per_launch": rows * bpr, "kernel_ms": star_avg_s * 1e3,
+                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                else "fallback 6800 GB/s", "traffic_source": tr.get("source") if tr else None}
+
+    # e2e: the same query through the C ABI with the fact columns coming from
+    # pinned host memory every step and the result read back to the host.
+    e2e = None
+    if not args.no_e2e:
+        used = {0: [0, 1, 2, 3], 1: [0, 4, 5], 2: [0, 5, 6, 7, 8]}[args.config]
+        pinned = {}
+        for c in used:
+            t = torch.empty(rows, dtype=torch.int32, pin_memory=True)
+            a = t.numpy()
+            a[:] = eng.read("lineorder", c)
+            pinned[c] = (t, a)
+        import copy
+        qp = copy.deepcopy(w.query)
+        qp.pre_pipeline_id[0] = "lineorder_e2e"
+        cols = [pinned[c][1] if c in pinned else None for c in range(len(w.fact_cols))]
+        eng.put("lineorder_e2e", cols)
+        eng.run(qp)
+        barrier()
+        h2d = sum(4 * rows for _ in used)
+        times = []
+        for _ in range(max(1, min(args.steps, 10))):
+            t0 = time.perf_counter()
+            eng.put("lineorder_e2e", cols)
+            eng.run(qp)
+            keys, sums = eng.result(qp.id, w.key_num)
+            times.append(time.perf_counter() - t0)
+        d2h = keys.nbytes + sums.nbytes
+        e2e_s = statistics.median(times)
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([e2e_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": rows * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+               "api": "svm_object_put (pinned host columns) + svm_run_pipeline + svm_object_read"}
+        eng.drop("lineorder_e2e")
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample = args.cpu_sample_rows or default_cpu_sample(args.config, threads)
+        rates, _, desc = cpu_reference_run(args.config, sample, 3, threads)
+        cpu = {"value": statistics.median(rates), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": desc}
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "int32",
+               "data": "synthetic (seeded counter-based generator on the device, star-schema shapes)",
+               "config": dict(workload_config(args.config, rows * world), join_mode=args.join_mode,
+                              rows_per_gpu=rows, parallelism=f"row shards x{world}"),
+               "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+               "clocks": clk, "dimension_build_s": build_s,
+               "hbm_frac_of_measured": roofline["frac"]}
+        print(json.dumps(out))
+    eng.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2])
+    ap.add_argument("--rows", type=int, default=None, help="fact rows per GPU (default: the config's)")
+    ap.add_argument("--cpu-sample-rows", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--join-mode", default="ref_compat", choices=["ref_compat", "exact"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        ours_arm(args)
+
+
+if __name__ == "__main__":
+    main()

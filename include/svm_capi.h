@@ -1,0 +1,182 @@
+/*
+ * svm_capi.h -- C ABI of the GB300 data plane for ShadowVM's query hot path:
+ * fused fact-table filter -> dimension hash-table build/probe -> group-by
+ * aggregate over columnar int32 tables, on one GPU (sm_103a).
+ *
+ * Plain C: opaque handles, pointers and sizes, no C++ or torch types.  Every
+ * call returns an svm_status; on failure svm_last_error() describes it.
+ * A context is used by one host thread at a time (the library serialises
+ * calls on a context with an internal mutex).
+ *
+ * What each entry point stands in for in the reference (paths are relative to
+ * the ShadowVM source tree):
+ *   svm_init / svm_destroy        ObjectStore ctor (object/store.cpp:13-36) + ResMgr::Init
+ *                                 (core/resource.cu:35-47) + ShadowVMService::Init (service/service.cu:17-21)
+ *   svm_object_*                  ObjectStore Create/Get/Destroy (object/store.cpp:49-91), RamObject
+ *                                 bulks (object/object.cpp:55-95), Object::To(DeviceMem) (object/object.cpp:194-294)
+ *   svm_run_pipeline              ShadowVMService::RunPipelineCMD (service/service.cu:25-63) ->
+ *                                 PipelineTest::Run (test/test.hpp:122-146) -> Pipeline ctor/Open/Run
+ *                                 (core/pipeline.cu:11-254) -> Query::Next (core/operator.cpp:121-187) ->
+ *                                 the generated per-row loop (codegen/template.cpp:61-89) ->
+ *                                 ReduceTask (core/pipeline.cu:360-472); result cached by pipeline
+ *                                 id like ShadowVMService::cached_obj (service/service.hpp:92)
+ *   svm_run_batch                 no counterpart: many RunPipelineCMD calls folded into one launch
+ */
+#ifndef SVM_CAPI_H_
+#define SVM_CAPI_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SVM_ABI_VERSION 1
+
+typedef enum svm_status {
+  SVM_OK = 0,
+  SVM_E_INVALID_ARG = 1,  /* malformed pipeline, bad id/column, wrong sizes */
+  SVM_E_UNSUPPORTED = 2,  /* outside the supported expression/operator set; no fallback runs */
+  SVM_E_OOM_BUDGET = 3,   /* the HBM budget (svm_config.hbm_budget_bytes) would be exceeded */
+  SVM_E_TIMEOUT = 4,      /* a bounded device wait gave up */
+  SVM_E_CUDA = 5,         /* a CUDA runtime call failed */
+  SVM_E_NOT_FOUND = 6,    /* unknown object / pipeline id (the RPC's CANCELLED case) */
+  SVM_E_DEVICE = 7        /* a kernel reported an error (e.g. integer division by zero) */
+} svm_status;
+
+/* Value types: the numbering of ValType in com/svm.proto:62-72. */
+enum { SVM_BYTE = 0, SVM_INT16 = 1, SVM_INT32 = 2, SVM_INT64 = 3, SVM_FLOAT16 = 4,
+       SVM_FLOAT32 = 5, SVM_FLOAT64 = 6, SVM_STRING = 7, SVM_TENSOR = 8 };
+
+/* Operator types: OperatorInfo.Type in com/svm.proto:102-111. */
+enum { SVM_OP_SOURCE = 0, SVM_OP_LOADER = 1, SVM_OP_FILTER = 2, SVM_OP_MAP = 3,
+       SVM_OP_REDUCEBY = 4, SVM_OP_SORTBY = 5, SVM_OP_JOINWITH = 6, SVM_OP_SINK = 7 };
+
+/* Join semantics.
+ * SVM_JOIN_REF_COMPAT: exactly the reference's CPU path.  A joined object
+ *   contributes only its first bulk (rows that came from the first
+ *   tuple_per_bulk source rows; core/pipeline.cu:91,295), and a dimension
+ *   row the reference's 10-step capped linear-probing table
+ *   (com/cpp/cpu-runtime.hpp:80-91, HashRate x tuple_per_bulk slots) fails to
+ *   insert is never matched.
+ * SVM_JOIN_EXACT: every dimension row is joinable.
+ * In both modes a key present more than once matches its first row, as the
+ * reference's Probe does (cpu-runtime.hpp:125-138). */
+enum { SVM_JOIN_REF_COMPAT = 0, SVM_JOIN_EXACT = 1 };
+
+typedef struct svm_config {
+  int device;                        /* CUDA device ordinal */
+  unsigned long long hbm_budget_bytes; /* device bytes the context may hold; 0 = no limit */
+  unsigned long long tuple_per_bulk; /* the reference's bulk size, Context::tuple_per_bulk_
+                                        (com/cpp/com.cu:13), default 2,000,000 */
+  int join_mode;                     /* SVM_JOIN_REF_COMPAT (default) or SVM_JOIN_EXACT */
+  int hash_char_signed;              /* 1 (default): hash key bytes as signed char, as the
+                                        x86 reference does; 0: unsigned (aarch64 build) */
+} svm_config;
+
+typedef struct svm_ctx svm_ctx;
+
+/* ---- context ------------------------------------------------------------ */
+void svm_config_default(svm_config* cfg);
+svm_status svm_init(const svm_config* cfg, svm_ctx** out);
+void svm_destroy(svm_ctx* ctx);
+const char* svm_last_error(const svm_ctx* ctx);
+int svm_abi_version(void);
+/* The cudaStream_t every library kernel of this context is launched on. */
+void* svm_stream(svm_ctx* ctx);
+/* Device bytes currently held by the context (objects, tables, scratch). */
+unsigned long long svm_bytes_in_use(const svm_ctx* ctx);
+
+/* ---- object store (device-resident int32/int64 columns) ------------------ */
+/* Create object `id` with `ncols` columns of `nrows` rows each.  types[c] is
+ * SVM_INT32 or SVM_INT64.  columns[c] points at nrows values in host memory
+ * (copied to the device) or, with columns_on_device != 0, in device memory
+ * (copied device to device).  columns == NULL leaves the columns zeroed.
+ * Replaces an existing object of the same id. */
+svm_status svm_object_put(svm_ctx* ctx, const char* id, int ncols, const int* types,
+                          unsigned long long nrows, const void* const* columns,
+                          int columns_on_device);
+/* Fill column `col` of an existing int32 object on the device with the seeded
+ * counter-based generator: value(i) = lo + ((mix(seed, stream, row0 + i) >> 32)
+ * * (hi - lo + 1)) >> 32 (splitmix64 output function), i.e. rows row0.. of an
+ * unbounded synthetic table.  With `lookup` non-NULL the drawn value v in
+ * [lo, hi] is replaced by lookup[v - lo] (lookup in host memory, hi - lo + 1
+ * entries). */
+svm_status svm_object_gen_uniform(svm_ctx* ctx, const char* id, int col, unsigned long long seed,
+                                  unsigned long long stream, unsigned long long row0, int lo, int hi,
+                                  const int* lookup);
+/* Zero-copy view: rows [row0, row0 + nrows) of object `base` as object `id`. */
+svm_status svm_object_view(svm_ctx* ctx, const char* id, const char* base,
+                           unsigned long long row0, unsigned long long nrows);
+svm_status svm_object_info(svm_ctx* ctx, const char* id, int* ncols, unsigned long long* nrows);
+svm_status svm_object_types(svm_ctx* ctx, const char* id, int* types, int max_cols);
+/* Copy rows [row0, row0 + n) of column `col` to host memory (4 or 8 bytes per value). */
+svm_status svm_object_read(svm_ctx* ctx, const char* id, int col, unsigned long long row0,
+                           unsigned long long n, void* host_out);
+/* Device address of column `col` (valid until the object is dropped/replaced). */
+svm_status svm_object_device_ptr(svm_ctx* ctx, const char* id, int col, void** dptr);
+svm_status svm_object_drop(svm_ctx* ctx, const char* id);
+
+/* ---- pipelines (PipelineInfo, com/svm.proto:101-144) ---------------------- */
+typedef struct svm_arg {
+  const char* key;   /* OperatorInfo.args key: predication, select, lkey, rkey, dim, metric ... */
+  const char* value;
+} svm_arg;
+
+typedef struct svm_column_desc { /* ColumnInfo (svm.proto:73-79) */
+  int type;                      /* SVM_INT32, SVM_INT64, SVM_STRING ... */
+  long long val_size;
+} svm_column_desc;
+
+typedef struct svm_operator {    /* OperatorInfo (svm.proto:101-123) */
+  int type;                      /* SVM_OP_* */
+  int nargs;
+  const svm_arg* args;
+  int ncols;                     /* output ObjectInfo's column_list */
+  const svm_column_desc* output;
+} svm_operator;
+
+typedef struct svm_pipeline {    /* PipelineInfo (svm.proto:137-144) */
+  const char* id;
+  int nops;
+  const svm_operator* ops;
+  int npre;
+  const char* const* pre_pipeline_id; /* [0] = source object, [1..] = joined objects */
+} svm_pipeline;
+
+/* Run one pipeline and store its output as object `pipe->id`.
+ *   Source/Filter/Map/Sink            -> filtered, projected, row-order-preserving
+ *                                        copy (the dimension-side pipelines)
+ *   Source/Filter/JoinWith.../ReduceBy/Sink -> fused scan/probe/aggregate; output
+ *                                        rows are the groups sorted by key:
+ *                                        key columns (int32) then one column
+ *                                        per metric, int64 when the Sink
+ *                                        declares Int64, else wrapped to int32.
+ * A missing pre_pipeline_id object returns SVM_E_NOT_FOUND. */
+svm_status svm_run_pipeline(svm_ctx* ctx, const svm_pipeline* pipe);
+
+/* Run n reduce pipelines as one batched persistent launch (shared scan of the
+ * resident fact columns, per-query predicates, probes and aggregate slots).
+ * Every output is stored as in svm_run_pipeline.  The result of each pipeline
+ * equals its result from svm_run_pipeline. */
+svm_status svm_run_batch(svm_ctx* ctx, int n, const svm_pipeline* pipes);
+
+/* ---- profiling -------------------------------------------------------------- */
+/* With profiling on, the library brackets each of its kernel launches with
+ * CUDA events on its stream.  svm_profile_read reports, for kernel class k
+ * (SVM_K_*), the number of launches and the summed event time in ms since the
+ * last reset. */
+enum { SVM_K_STAR = 0, SVM_K_SELECT = 1, SVM_K_BUILD = 2, SVM_K_FINALIZE = 3, SVM_K_BATCH = 4,
+       SVM_K_OTHER = 5, SVM_K_COUNT = 6 };
+svm_status svm_profile_enable(svm_ctx* ctx, int on);
+svm_status svm_profile_reset(svm_ctx* ctx);
+svm_status svm_profile_read(svm_ctx* ctx, int kernel_class, unsigned long long* launches,
+                            double* total_ms);
+/* Number of CUDA kernels this library has launched in the process so far. */
+unsigned long long svm_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SVM_CAPI_H_ */

@@ -1,0 +1,417 @@
+// The C ABI (include/svm_capi.h): context, object store, profiling.
+#include <climits>
+#include <cstring>
+
+#include "ctx.h"
+#include "kernels.h"
+
+namespace svm {
+
+DevBuf::~DevBuf() {
+  if (p) {
+    cudaFree(p);
+    if (ctx) ctx->in_use -= bytes;
+  }
+}
+
+svm_status Ctx::cuda_fail(cudaError_t e, const char* what) {
+  err = std::string(what) + ": " + cudaGetErrorString(e);
+  return SVM_E_CUDA;
+}
+
+svm_status Ctx::alloc(size_t bytes, DevBufPtr* out, bool zero) {
+  if (bytes == 0) bytes = 256;
+  if (cfg.hbm_budget_bytes && in_use + bytes > cfg.hbm_budget_bytes)
+    return fail(SVM_E_OOM_BUDGET, "HBM budget exceeded: " + std::to_string(in_use) + " + " +
+                                      std::to_string(bytes) + " > " + std::to_string(cfg.hbm_budget_bytes));
+  auto b = std::make_shared<DevBuf>();
+  cudaError_t e = cudaMalloc(&b->p, bytes);
+  if (e != cudaSuccess) {
+    b->p = nullptr;
+    cudaGetLastError();
+    return cuda_fail(e, "cudaMalloc");
+  }
+  b->ctx = this;
+  b->bytes = bytes;
+  in_use += bytes;
+  if (zero && (e = cudaMemsetAsync(b->p, 0, bytes, stream)) != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  *out = b;
+  return SVM_OK;
+}
+
+svm_status Ctx::scratch_reserve(size_t bytes) {
+  if (scratch && scratch->bytes >= bytes) return SVM_OK;
+  if (scratch) {
+    cudaError_t e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  }
+  scratch.reset();
+  size_t want = bytes < (64u << 20) ? (64u << 20) : bytes + (bytes >> 2);
+  return alloc(want, &scratch);
+}
+
+svm_status Ctx::scratch_take(size_t bytes, void** out) {
+  size_t off = (scratch_used + 255) & ~size_t(255);
+  if (!scratch || off + bytes > scratch->bytes)
+    return fail(SVM_E_INVALID_ARG, "internal: scratch arena too small");
+  *out = (char*)scratch->p + off;
+  scratch_used = off + bytes;
+  return SVM_OK;
+}
+
+svm_status Ctx::column_stats(const ObjectPtr& o, int c, ColStats* out) {
+  if ((int)o->stats.size() < o->ncols) o->stats.resize(o->ncols);
+  if (!o->stats[c].valid) {
+    if (o->types[c] != SVM_INT32) return fail(SVM_E_UNSUPPORTED, "column statistics need an int32 column");
+    int32_t h[2] = {INT_MAX, INT_MIN};
+    DevBufPtr d;
+    svm_status st = alloc(8, &d);
+    if (st) return st;
+    cudaError_t e = cudaMemcpyAsync(d->p, h, 8, cudaMemcpyHostToDevice, stream);
+    if (!e) e = launch_minmax((const int32_t*)o->col(c), o->nrows, (int32_t*)d->p, stream);
+    if (!e) e = cudaMemcpyAsync(h, d->p, 8, cudaMemcpyDeviceToHost, stream);
+    if (!e) e = cudaStreamSynchronize(stream);
+    if (e) return cuda_fail(e, "column statistics");
+    o->stats[c].valid = true;
+    o->stats[c].min = h[0];
+    o->stats[c].max = h[1];
+  }
+  *out = o->stats[c];
+  return SVM_OK;
+}
+
+void Ctx::prof_begin(int cls, cudaEvent_t* a) {
+  *a = nullptr;
+  if (!profiling) return;
+  if (event_pool.empty()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    event_pool.push_back(e);
+  }
+  *a = event_pool.back();
+  event_pool.pop_back();
+  cudaEventRecord(*a, stream);
+  (void)cls;
+}
+
+void Ctx::prof_end(int cls, cudaEvent_t a) {
+  if (!profiling || !a) return;
+  cudaEvent_t b;
+  if (event_pool.empty()) {
+    cudaEventCreate(&b);
+  } else {
+    b = event_pool.back();
+    event_pool.pop_back();
+  }
+  cudaEventRecord(b, stream);
+  pending.push_back({cls, a, b});
+}
+
+void Ctx::prof_collect() {
+  if (pending.empty()) return;
+  cudaStreamSynchronize(stream);
+  for (auto& pe : pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, pe.a, pe.b);
+    prof_launches[pe.cls]++;
+    prof_ms[pe.cls] += ms;
+    event_pool.push_back(pe.a);
+    event_pool.push_back(pe.b);
+  }
+  pending.clear();
+}
+
+}  // namespace svm
+
+using svm::Ctx;
+using svm::ObjectPtr;
+
+static Ctx* C(svm_ctx* c) { return &c->impl; }
+
+extern "C" {
+
+int svm_abi_version(void) { return SVM_ABI_VERSION; }
+
+void svm_config_default(svm_config* cfg) {
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->device = 0;
+  cfg->hbm_budget_bytes = 0;
+  cfg->tuple_per_bulk = 2000000ull;  // com/cpp/com.cu:13
+  cfg->join_mode = SVM_JOIN_REF_COMPAT;
+  cfg->hash_char_signed = 1;
+}
+
+svm_status svm_init(const svm_config* cfg, svm_ctx** out) {
+  if (!out) return SVM_E_INVALID_ARG;
+  *out = nullptr;
+  svm_config c;
+  if (cfg)
+    c = *cfg;
+  else
+    svm_config_default(&c);
+  if (c.tuple_per_bulk == 0 || c.tuple_per_bulk > (1ull << 31) / svm::kHashRate) return SVM_E_INVALID_ARG;
+  if (c.join_mode != SVM_JOIN_REF_COMPAT && c.join_mode != SVM_JOIN_EXACT) return SVM_E_INVALID_ARG;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || c.device < 0 || c.device >= n) {
+    cudaGetLastError();
+    return SVM_E_CUDA;
+  }
+  if (cudaSetDevice(c.device) != cudaSuccess) return SVM_E_CUDA;
+  svm_ctx* h = new svm_ctx();
+  Ctx* x = &h->impl;
+  x->cfg = c;
+  x->device = c.device;
+  if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&x->d_error, sizeof(int)) != cudaSuccess ||
+      cudaMemset(x->d_error, 0, sizeof(int)) != cudaSuccess) {
+    delete h;
+    return SVM_E_CUDA;
+  }
+  *out = h;
+  return SVM_OK;
+}
+
+void svm_destroy(svm_ctx* c) {
+  if (!c) return;
+  Ctx* x = C(c);
+  cudaSetDevice(x->device);
+  if (x->stream) cudaStreamSynchronize(x->stream);
+  x->prof_collect();
+  x->objects.clear();
+  x->dim_cache.clear();
+  x->scratch.reset();
+  for (auto e : x->event_pool) cudaEventDestroy(e);
+  if (x->d_error) cudaFree(x->d_error);
+  if (x->stream) cudaStreamDestroy(x->stream);
+  delete c;
+}
+
+const char* svm_last_error(const svm_ctx* c) { return c ? c->impl.err.c_str() : "null context"; }
+
+void* svm_stream(svm_ctx* c) { return c ? (void*)c->impl.stream : nullptr; }
+
+unsigned long long svm_bytes_in_use(const svm_ctx* c) { return c ? c->impl.in_use : 0; }
+
+svm_status svm_object_put(svm_ctx* c, const char* id, int ncols, const int* types,
+                          unsigned long long nrows, const void* const* columns, int on_device) {
+  if (!c || !id || ncols <= 0 || ncols > 64 || !types) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  cudaSetDevice(x->device);
+  auto o = std::make_shared<svm::Object>();
+  o->id = id;
+  o->version = x->next_version++;
+  o->ncols = ncols;
+  o->nrows = nrows;
+  o->has_bulks = nrows > 0;
+  o->bulk0_rows = nrows < x->cfg.tuple_per_bulk ? nrows : x->cfg.tuple_per_bulk;
+  o->source_rows = nrows;
+  unsigned long long padded = (nrows + 63) / 64 * 64 + 64;
+  // Replacing an object of the same shape that no view shares: reuse its storage.
+  ObjectPtr old = x->find(id);
+  bool reuse = old && old->ncols == ncols && old->nrows == nrows && old->row0 == 0;
+  for (int k = 0; reuse && k < ncols; k++)
+    reuse = old->types[k] == types[k] && old->storage[k].use_count() == 1;
+  for (int k = 0; k < ncols; k++) {
+    if (types[k] != SVM_INT32 && types[k] != SVM_INT64)
+      return x->fail(SVM_E_UNSUPPORTED, "object columns must be Int32 or Int64");
+    o->types.push_back(types[k]);
+    svm::DevBufPtr b;
+    size_t el = types[k] == SVM_INT64 ? 8 : 4;
+    if (reuse) {
+      b = old->storage[k];
+      if (!(columns && columns[k] && nrows)) {
+        cudaError_t e = cudaMemsetAsync(b->p, 0, b->bytes, x->stream);
+        if (e) return x->cuda_fail(e, "cudaMemsetAsync");
+      }
+    } else {
+      svm_status st = x->alloc(padded * el, &b, true);
+      if (st) return st;
+    }
+    if (columns && columns[k] && nrows) {
+      cudaError_t e = cudaMemcpyAsync(b->p, columns[k], nrows * el,
+                                      on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                      x->stream);
+      if (e) return x->cuda_fail(e, "cudaMemcpyAsync");
+    }
+    o->storage.push_back(b);
+  }
+  cudaError_t e = cudaStreamSynchronize(x->stream);
+  if (e) return x->cuda_fail(e, "object upload");
+  x->objects[id] = o;
+  return SVM_OK;
+}
+
+svm_status svm_object_gen_uniform(svm_ctx* c, const char* id, int col, unsigned long long seed,
+                                  unsigned long long stream, unsigned long long row0, int lo, int hi,
+                                  const int* lookup) {
+  if (!c || !id || hi < lo) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  cudaSetDevice(x->device);
+  ObjectPtr o = x->find(id);
+  if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
+  if (col < 0 || col >= o->ncols || o->types[col] != SVM_INT32)
+    return x->fail(SVM_E_INVALID_ARG, "gen_uniform needs an int32 column");
+  svm::DevBufPtr lut;
+  if (lookup) {
+    size_t n = (size_t)((long long)hi - lo + 1) * 4;
+    svm_status st = x->alloc(n, &lut);
+    if (st) return st;
+    cudaError_t e = cudaMemcpyAsync(lut->p, lookup, n, cudaMemcpyHostToDevice, x->stream);
+    if (e) return x->cuda_fail(e, "cudaMemcpyAsync");
+  }
+  cudaEvent_t ev;
+  x->prof_begin(SVM_K_OTHER, &ev);
+  cudaError_t e = svm::launch_gen_uniform((int32_t*)o->col(col), o->nrows, seed, stream, row0, lo, hi,
+                                          lut ? (const int32_t*)lut->p : nullptr, x->stream);
+  x->prof_end(SVM_K_OTHER, ev);
+  if (!e) e = cudaStreamSynchronize(x->stream);
+  if (e) return x->cuda_fail(e, "gen_uniform");
+  if ((int)o->stats.size() > col) o->stats[col].valid = false;
+  o->version = x->next_version++;
+  return SVM_OK;
+}
+
+svm_status svm_object_view(svm_ctx* c, const char* id, const char* base, unsigned long long row0,
+                           unsigned long long nrows) {
+  if (!c || !id || !base) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  ObjectPtr b = x->find(base);
+  if (!b) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + base);
+  if (row0 > b->nrows || nrows > b->nrows - row0) return x->fail(SVM_E_INVALID_ARG, "view out of range");
+  auto o = std::make_shared<svm::Object>(*b);
+  o->id = id;
+  o->version = x->next_version++;
+  o->row0 = b->row0 + row0;
+  o->nrows = nrows;
+  o->has_bulks = nrows > 0;
+  o->bulk0_rows = nrows < x->cfg.tuple_per_bulk ? nrows : x->cfg.tuple_per_bulk;
+  o->source_rows = nrows;
+  // Column statistics of the base bound the view's values.
+  x->objects[id] = o;
+  return SVM_OK;
+}
+
+svm_status svm_object_info(svm_ctx* c, const char* id, int* ncols, unsigned long long* nrows) {
+  if (!c || !id) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  ObjectPtr o = x->find(id);
+  if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
+  if (ncols) *ncols = o->ncols;
+  if (nrows) *nrows = o->nrows;
+  return SVM_OK;
+}
+
+svm_status svm_object_types(svm_ctx* c, const char* id, int* types, int max_cols) {
+  if (!c || !id || !types) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  ObjectPtr o = x->find(id);
+  if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
+  for (int k = 0; k < o->ncols && k < max_cols; k++) types[k] = o->types[k];
+  return SVM_OK;
+}
+
+svm_status svm_object_read(svm_ctx* c, const char* id, int col, unsigned long long row0,
+                           unsigned long long n, void* host_out) {
+  if (!c || !id || (!host_out && n)) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  cudaSetDevice(x->device);
+  ObjectPtr o = x->find(id);
+  if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
+  if (col < 0 || col >= o->ncols || row0 > o->nrows || n > o->nrows - row0)
+    return x->fail(SVM_E_INVALID_ARG, "read out of range");
+  if (!n) return SVM_OK;
+  size_t el = o->elem(col);
+  cudaError_t e = cudaMemcpyAsync(host_out, o->col(col) + row0 * el, n * el, cudaMemcpyDeviceToHost, x->stream);
+  if (!e) e = cudaStreamSynchronize(x->stream);
+  if (e) return x->cuda_fail(e, "object read");
+  return SVM_OK;
+}
+
+svm_status svm_object_device_ptr(svm_ctx* c, const char* id, int col, void** dptr) {
+  if (!c || !id || !dptr) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  ObjectPtr o = x->find(id);
+  if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
+  if (col < 0 || col >= o->ncols) return x->fail(SVM_E_INVALID_ARG, "bad column");
+  *dptr = o->col(col);
+  return SVM_OK;
+}
+
+svm_status svm_object_drop(svm_ctx* c, const char* id) {
+  if (!c || !id) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  cudaSetDevice(x->device);
+  auto it = x->objects.find(id);
+  if (it == x->objects.end()) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
+  cudaStreamSynchronize(x->stream);
+  x->objects.erase(it);
+  // Tables built over the dropped object are keyed by its version; drop them too.
+  for (auto d = x->dim_cache.begin(); d != x->dim_cache.end();) {
+    if (d->first.compare(0, std::strlen(id) + 1, std::string(id) + "#") == 0)
+      d = x->dim_cache.erase(d);
+    else
+      ++d;
+  }
+  return SVM_OK;
+}
+
+svm_status svm_run_pipeline(svm_ctx* c, const svm_pipeline* p) {
+  if (!c || !p) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  cudaSetDevice(x->device);
+  x->err.clear();
+  return svm::run_pipeline(x, p);
+}
+
+svm_status svm_run_batch(svm_ctx* c, int n, const svm_pipeline* p) {
+  if (!c || (n > 0 && !p) || n < 0) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  cudaSetDevice(x->device);
+  x->err.clear();
+  return svm::run_batch(x, n, p);
+}
+
+unsigned long long svm_kernel_launches(void) { return svm::launches_total(); }
+
+svm_status svm_profile_enable(svm_ctx* c, int on) {
+  if (!c) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  x->prof_collect();
+  x->profiling = on != 0;
+  return SVM_OK;
+}
+
+svm_status svm_profile_reset(svm_ctx* c) {
+  if (!c) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  x->prof_collect();
+  for (int k = 0; k < SVM_K_COUNT; k++) {
+    x->prof_launches[k] = 0;
+    x->prof_ms[k] = 0;
+  }
+  return SVM_OK;
+}
+
+svm_status svm_profile_read(svm_ctx* c, int cls, unsigned long long* launches, double* total_ms) {
+  if (!c || cls < 0 || cls >= SVM_K_COUNT) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  x->prof_collect();
+  if (launches) *launches = x->prof_launches[cls];
+  if (total_ms) *total_ms = x->prof_ms[cls];
+  return SVM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,132 @@
+// Host-side state of one data-plane context: the device object store, the
+// dimension-table cache, scratch memory and profiling.  Mirrors the reference's
+// ObjectStore (object/store.cpp:13-91), RamObject bulks (object/object.cpp:55-95)
+// and the service's cached_obj map (service/service.hpp:92), with every column
+// resident in HBM.
+#pragma once
+
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/svm_capi.h"
+#include "svm_internal.h"
+
+namespace svm {
+
+struct Ctx;
+
+// A device allocation charged to the context's HBM budget.
+struct DevBuf {
+  Ctx* ctx = nullptr;
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf();
+};
+using DevBufPtr = std::shared_ptr<DevBuf>;
+
+struct ColStats {
+  bool valid = false;
+  int32_t min = 0, max = 0;
+};
+
+// A columnar object.  Columns are int32 or int64; each column's storage is
+// padded to a multiple of 64 rows (+64 rows) so the scan's 16-byte group loads
+// never leave the allocation.  A view shares its base object's storage.
+struct Object {
+  std::string id;
+  unsigned long long version = 0;
+  int ncols = 0;
+  std::vector<int> types;
+  unsigned long long nrows = 0;
+  unsigned long long row0 = 0;                // rows skipped in the base storage (views)
+  std::vector<DevBufPtr> storage;             // base allocation per column
+  // The reference keeps objects as bulks of tuple_per_bulk rows and joins only
+  // against bulk 0 of a joined object (core/pipeline.cu:91,295).
+  bool has_bulks = false;
+  unsigned long long bulk0_rows = 0;
+  // Rows of the object this one was filtered from (a dimension pipeline's
+  // source); estimates how selective a join against it is.
+  unsigned long long source_rows = 0;
+  std::vector<ColStats> stats;
+
+  char* base(int c) const { return (char*)storage[c]->p; }
+  size_t elem(int c) const { return types[c] == SVM_INT64 ? 8 : 4; }
+  char* col(int c) const { return base(c) + row0 * elem(c); }
+};
+using ObjectPtr = std::shared_ptr<Object>;
+
+// A built dimension table plus what the planner needs to know about it.
+struct DimTable {
+  DimDesc desc{};
+  DevBufPtr words;
+  unsigned long long live = 0;                // rows inserted
+  unsigned long long rows_considered = 0;     // rows of the object the build looked at
+  std::vector<int> pay_cols;                  // object columns behind desc.pay[]
+  std::vector<int32_t> pay_min, pay_max;      // over inserted rows
+  int32_t key_min = 0, key_max = 0;
+  size_t bytes() const { return words ? words->bytes : 0; }
+};
+using DimTablePtr = std::shared_ptr<DimTable>;
+
+struct ProfEvent {
+  int cls;
+  cudaEvent_t a, b;
+};
+
+struct Ctx {
+  svm_config cfg{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::recursive_mutex mu;
+  std::string err;
+  size_t in_use = 0;
+  unsigned long long next_version = 1;
+  std::map<std::string, ObjectPtr> objects;
+  std::map<std::string, DimTablePtr> dim_cache;
+  int* d_error = nullptr;                     // device error word
+  // Grow-only scratch arena, carved per operation.
+  DevBufPtr scratch;
+  size_t scratch_used = 0;
+  // Profiling.
+  bool profiling = false;
+  std::vector<ProfEvent> pending;
+  std::vector<cudaEvent_t> event_pool;
+  unsigned long long prof_launches[SVM_K_COUNT] = {};
+  double prof_ms[SVM_K_COUNT] = {};
+
+  svm_status fail(svm_status s, const std::string& m) {
+    err = m;
+    return s;
+  }
+  svm_status cuda_fail(cudaError_t e, const char* what);
+
+  // Allocation charged to the budget (zero-filled when `zero`).
+  svm_status alloc(size_t bytes, DevBufPtr* out, bool zero = false);
+  // Scratch: reset() then take() pieces; valid until the next reset().
+  void scratch_reset() { scratch_used = 0; }
+  svm_status scratch_take(size_t bytes, void** out);
+  svm_status scratch_reserve(size_t bytes);
+
+  ObjectPtr find(const std::string& id) {
+    auto it = objects.find(id);
+    return it == objects.end() ? nullptr : it->second;
+  }
+  svm_status column_stats(const ObjectPtr& o, int c, ColStats* out);
+
+  void prof_begin(int cls, cudaEvent_t* a);
+  void prof_end(int cls, cudaEvent_t a);
+  void prof_collect();
+};
+
+// Pipelines (pipeline.cpp).
+svm_status run_pipeline(Ctx* ctx, const svm_pipeline* p);
+svm_status run_batch(Ctx* ctx, int n, const svm_pipeline* p);
+
+}  // namespace svm
+
+struct svm_ctx {
+  svm::Ctx impl;
+};

@@ -1,0 +1,81 @@
+// Host-callable launchers for the library's CUDA kernels.  Every launcher
+// enqueues on `stream` and returns the launch's cudaError_t; none synchronizes.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "svm_internal.h"
+
+namespace svm {
+
+int num_sms();
+// Process-wide count of kernel launches (every <<<>>> site calls this).
+void note_launch(int n = 1);
+unsigned long long launches_total();
+
+// ---- utilities (kern_util.cu)
+cudaError_t launch_gen_uniform(int32_t* out, unsigned long long n, unsigned long long seed,
+                               unsigned long long stream_id, unsigned long long row0, int lo, int hi,
+                               const int32_t* lookup, cudaStream_t s);
+// min/max of n int32 values into out[0] (min) out[1] (max); out must be preset
+// to {INT_MAX, INT_MIN}.
+cudaError_t launch_minmax(const int32_t* in, unsigned long long n, int32_t* out, cudaStream_t s);
+// Exclusive prefix sum of n uint32 values into n+1 uint64 values (out[n] = total).
+// `tmp` needs scan_tmp_words(n) uint64 words.
+size_t scan_tmp_words(unsigned long long n);
+cudaError_t launch_exclusive_scan(const uint32_t* in, unsigned long long n, unsigned long long* out,
+                                  unsigned long long* tmp, cudaStream_t s);
+// Inclusive running maximum of n int32 values (in place allowed).
+cudaError_t launch_inclusive_max(const int32_t* in, unsigned long long n, int32_t* out,
+                                 int32_t* tmp, cudaStream_t s);
+size_t max_tmp_words(unsigned long long n);
+
+// ---- select pipelines (kern_dim.cu)
+// Pass 1: per-tile counts of rows passing the conjuncts; pass 2: order-preserving write.
+unsigned long long select_tiles(long long nrows);
+cudaError_t launch_select_count(const SelectParams& p, cudaStream_t s);
+cudaError_t launch_select_write(const SelectParams& p, cudaStream_t s);
+
+// ---- dimension tables (kern_dim.cu)
+struct BuildInput {
+  const int32_t* key;               // key column, rows [0, n)
+  long long n;
+  int npay;
+  const int32_t* pay[kMaxKeys + 2 * kMaxMetrics];
+  const uint8_t* dropped;           // rows to leave out (may be null)
+};
+
+// Reference-table emulation: marks in `dropped` (n bytes, zeroed by the call)
+// every row the sequential 10-step capped insert over ht_size slots
+// (com/cpp/com.hpp:168-174, cpu-runtime.hpp:80-91) leaves out.
+// `scratch` must hold refcompat_scratch_bytes(n, ht_size) bytes.
+size_t refcompat_scratch_bytes(long long n, unsigned ht_size);
+cudaError_t launch_refcompat(const int32_t* key, long long n, unsigned ht_size, int signed_char,
+                             uint8_t* dropped, void* scratch, cudaStream_t s);
+
+// Stats of the rows that will be inserted: out[0..1] key min/max, out[2+2f..3+2f]
+// payload f min/max, out[2+2*npay] = number of rows inserted (as int32 bit pattern).
+cudaError_t launch_build_stats(const BuildInput& in, int32_t* out, cudaStream_t s);
+
+// Dense table: `owner` (span int32, scratch) and `words` (table_words) are
+// written; rows collide on a key -> the lowest row wins.
+cudaError_t launch_build_dense(const BuildInput& in, const DimDesc& d, int32_t* owner,
+                               uint32_t* words, cudaStream_t s);
+// Hash table: `slots` (cap uint64, scratch) then `words` (2*cap).
+cudaError_t launch_build_hash(const BuildInput& in, const DimDesc& d, unsigned long long* slots,
+                              uint32_t* words, int* error, cudaStream_t s);
+
+// ---- fused star query (kern_star.cu)
+cudaError_t launch_star(const StarParams& p, int grid, int block, size_t smem, cudaStream_t s);
+int star_block_size();
+int star_grid_size(const StarParams& p, size_t smem);
+size_t star_smem_bytes(const StarParams& p);
+// Compact non-empty groups in key order: writes keys (nkeys int32 columns),
+// metric columns (int64 or int32 per `wide`), and out_count.
+cudaError_t launch_finalize_dense(const StarParams& p, int32_t* const* key_out, void* const* met_out,
+                                  const int* wide, unsigned long long* flags_tmp,
+                                  unsigned long long* scan_tmp, unsigned long long* out_count,
+                                  cudaStream_t s);
+
+}  // namespace svm

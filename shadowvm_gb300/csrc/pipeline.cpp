@@ -1,0 +1,833 @@
+// Pipeline binding, planning and execution.
+//
+// bind()          mirrors Pipeline::Pipeline (core/pipeline.cu:11-80): operator
+//                 dispatch and expression binding out of the PipelineInfo.
+// run_select()    Source/Filter/Map/Sink pipelines (the dimension-side
+//                 pipelines, e.g. example/run_SSB_Q31.cu:11-74): one
+//                 order-preserving filter+project pass on the device.
+// run_star()      Source/Filter/JoinWith/ReduceBy/Sink pipelines: dimension
+//                 tables built (and cached) the way Pipeline::Open does
+//                 (core/pipeline.cu:82-137) but on the device, then the fused
+//                 scan of kern_star.cu replacing the generated loop and
+//                 ReduceTask (core/pipeline.cu:262-472).
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <set>
+
+#include "ctx.h"
+#include "expr.h"
+#include "kernels.h"
+
+namespace svm {
+
+namespace {
+
+struct Bound {
+  std::string id;
+  std::vector<std::string> select_exp, filter_exp, metric_exp;
+  std::vector<ColRef> reduce_key, join_lkey, join_rkey;
+  bool is_reduce = false;
+  bool has_map = false;
+  std::vector<svm_column_desc> sink;
+};
+
+const char* arg_of(const svm_operator& op, const char* key) {
+  for (int k = 0; k < op.nargs; k++)
+    if (op.args[k].key && std::strcmp(op.args[k].key, key) == 0) return op.args[k].value ? op.args[k].value : "";
+  return nullptr;
+}
+
+svm_status bind(Ctx* x, const svm_pipeline* p, Bound* b) {
+  b->id = p->id ? p->id : "";
+  if (b->id.empty()) return x->fail(SVM_E_INVALID_ARG, "pipeline id is empty");
+  bool has_sink = false;
+  for (int i = 0; i < p->nops; i++) {
+    const svm_operator& op = p->ops[i];
+    std::string err;
+    switch (op.type) {
+      case SVM_OP_SOURCE:
+        break;
+      case SVM_OP_LOADER:
+        return x->fail(SVM_E_UNSUPPORTED, "Loader (text parsing) pipelines are not part of this data plane; "
+                                          "put columns with svm_object_put");
+      case SVM_OP_SINK:
+        has_sink = true;
+        b->sink.assign(op.output, op.output + op.ncols);
+        break;
+      case SVM_OP_MAP: {
+        const char* s = arg_of(op, "select");
+        if (!s) return x->fail(SVM_E_INVALID_ARG, "Map without 'select'");
+        b->select_exp = str_split(s, ",");
+        b->has_map = true;
+        break;
+      }
+      case SVM_OP_FILTER: {
+        const char* s = arg_of(op, "predication");
+        if (!s) return x->fail(SVM_E_INVALID_ARG, "Filter without 'predication'");
+        b->filter_exp.push_back(s);
+        break;
+      }
+      case SVM_OP_REDUCEBY: {
+        const char* m = arg_of(op, "metric");
+        if (!m) return x->fail(SVM_E_INVALID_ARG, "ReduceBy without 'metric'");
+        b->metric_exp = str_split(m, ",");
+        const char* d = arg_of(op, "dim");
+        if (d) {
+          for (auto& e : str_split(d, ",")) {
+            ColRef r;
+            if (!parse_key_index(e, &r, &err)) return x->fail(SVM_E_INVALID_ARG, "ReduceBy dim: " + err);
+            b->reduce_key.push_back(r);
+          }
+        }
+        b->is_reduce = true;
+        break;
+      }
+      case SVM_OP_JOINWITH: {
+        const char* l = arg_of(op, "lkey");
+        const char* r = arg_of(op, "rkey");
+        if (!l || !r) return x->fail(SVM_E_INVALID_ARG, "JoinWith needs 'lkey' and 'rkey'");
+        ColRef lr, rr;
+        if (!parse_key_index(l, &lr, &err) || !parse_key_index(r, &rr, &err))
+          return x->fail(SVM_E_INVALID_ARG, "JoinWith: " + err);
+        b->join_lkey.push_back(lr);
+        b->join_rkey.push_back(rr);
+        break;
+      }
+      case SVM_OP_SORTBY:
+        break;  // ignored by the reference as well (core/pipeline.cu:69-71)
+      default:
+        return x->fail(SVM_E_INVALID_ARG, "unknown operator type " + std::to_string(op.type));
+    }
+  }
+  if (!has_sink) return x->fail(SVM_E_INVALID_ARG, "pipeline has no Sink");
+  return SVM_OK;
+}
+
+std::string join_filters(const std::vector<std::string>& f) {
+  // Filters are concatenated with "&&", no parentheses (codegen/codegen.cpp:100-110).
+  std::string s;
+  for (size_t i = 0; i < f.size(); i++) {
+    if (i) s += "&&";
+    s += f[i];
+  }
+  return s;
+}
+
+int ceil_log2(unsigned long long v) {  // bits to hold values 0..v-1
+  int b = 0;
+  while (b < 64 && (1ull << b) < v) b++;
+  return b;
+}
+
+svm_status sync_and_check(Ctx* x, const char* what) {
+  cudaError_t e = cudaStreamSynchronize(x->stream);
+  if (e) return x->cuda_fail(e, what);
+  int h = 0;
+  e = cudaMemcpy(&h, x->d_error, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e) return x->cuda_fail(e, what);
+  if (h) {
+    cudaMemset(x->d_error, 0, sizeof(int));
+    const char* m = h == 1 ? "integer division by zero in an expression"
+                           : h == 2 ? "dimension hash table overflow"
+                                    : "group key outside its computed range";
+    return x->fail(SVM_E_DEVICE, std::string(what) + ": " + m);
+  }
+  return SVM_OK;
+}
+
+ObjectPtr new_result_object(Ctx* x, const std::string& id, const std::vector<int>& types,
+                            unsigned long long nrows, svm_status* st) {
+  auto o = std::make_shared<Object>();
+  o->id = id;
+  o->version = x->next_version++;
+  o->ncols = (int)types.size();
+  o->types = types;
+  o->nrows = nrows;
+  o->source_rows = nrows;
+  unsigned long long padded = (nrows + 63) / 64 * 64 + 64;
+  for (int t : types) {
+    DevBufPtr b;
+    *st = x->alloc(padded * (t == SVM_INT64 ? 8 : 4), &b, true);
+    if (*st) return nullptr;
+    o->storage.push_back(b);
+  }
+  *st = SVM_OK;
+  return o;
+}
+
+// ============================================================ select pipelines
+svm_status run_select(Ctx* x, const Bound& b, const ObjectPtr& src) {
+  if (!b.join_rkey.empty())
+    return x->fail(SVM_E_UNSUPPORTED, "JoinWith followed by Map (a join without ReduceBy) is not supported");
+  if (!b.has_map) return x->fail(SVM_E_UNSUPPORTED, "a pipeline without ReduceBy needs a Map");
+  std::string err;
+  std::vector<Expr> proj(b.select_exp.size());
+  std::vector<ColRef> opnds;
+  for (size_t i = 0; i < b.select_exp.size(); i++) {
+    if (!parse_expr(b.select_exp[i], &proj[i], &err))
+      return x->fail(err.rfind("unsupported", 0) == 0 ? SVM_E_UNSUPPORTED : SVM_E_INVALID_ARG,
+                     "select '" + b.select_exp[i] + "': " + err);
+    collect_refs(proj[i], proj[i].root, &opnds);
+  }
+  Expr pred;
+  bool has_pred = !b.filter_exp.empty();
+  if (has_pred) {
+    std::string t = join_filters(b.filter_exp);
+    if (!parse_expr(t, &pred, &err))
+      return x->fail(err.rfind("unsupported", 0) == 0 ? SVM_E_UNSUPPORTED : SVM_E_INVALID_ARG,
+                     "predication '" + t + "': " + err);
+    collect_refs(pred, pred.root, &opnds);
+  }
+  if (b.select_exp.size() > 16) return x->fail(SVM_E_UNSUPPORTED, "more than 16 projected columns");
+  if (opnds.size() > 16) return x->fail(SVM_E_UNSUPPORTED, "more than 16 input columns referenced");
+  for (auto& r : opnds) {
+    if (r.obj != 0) return x->fail(SVM_E_INVALID_ARG, "Map/Filter references object " + std::to_string(r.obj) +
+                                                          " but the pipeline joins nothing");
+    if (r.col < 0 || r.col >= src->ncols) return x->fail(SVM_E_INVALID_ARG, "column out of range");
+    if (src->types[r.col] != SVM_INT32) return x->fail(SVM_E_UNSUPPORTED, "only int32 input columns");
+  }
+  for (size_t i = 0; i < b.select_exp.size(); i++) {
+    if (i >= b.sink.size()) return x->fail(SVM_E_INVALID_ARG, "Sink schema has fewer columns than the Map");
+    if (b.sink[i].type != SVM_INT32)
+      return x->fail(SVM_E_UNSUPPORTED, "projected columns must be declared Int32");
+  }
+  SelectParams sp{};
+  sp.ncols_in = (int)opnds.size();
+  for (size_t k = 0; k < opnds.size(); k++) sp.cols[k] = (const int32_t*)src->col(opnds[k].col);
+  sp.nrows = (long long)src->nrows;
+  sp.error = x->d_error;
+  if (has_pred) {
+    std::vector<int> conj;
+    flatten_and(pred, pred.root, &conj);
+    if (conj.size() <= 4) {
+      for (int c : conj)
+        if (!compile_prog(pred, c, opnds, &sp.pred[sp.npred++], &err)) return x->fail(SVM_E_UNSUPPORTED, err);
+    } else if (!compile_prog(pred, pred.root, opnds, &sp.pred[sp.npred++], &err)) {
+      return x->fail(SVM_E_UNSUPPORTED, err);
+    }
+  }
+  sp.nout = (int)proj.size();
+  for (size_t i = 0; i < proj.size(); i++)
+    if (!compile_prog(proj[i], proj[i].root, opnds, &sp.proj[i], &err)) return x->fail(SVM_E_UNSUPPORTED, err);
+
+  unsigned long long tiles = select_tiles(sp.nrows);
+  x->scratch_reset();
+  size_t need = 4 * (tiles + 1) + 8 * (tiles + 2) + 8 * scan_tmp_words(tiles) + 8 + 4096;
+  svm_status st = x->scratch_reserve(need);
+  if (st) return st;
+  void *tc, *to, *tt, *b0;
+  if ((st = x->scratch_take(4 * (tiles + 1), &tc)) || (st = x->scratch_take(8 * (tiles + 2), &to)) ||
+      (st = x->scratch_take(8 * scan_tmp_words(tiles), &tt)) || (st = x->scratch_take(8, &b0)))
+    return st;
+  sp.tile_count = (unsigned int*)tc;
+  sp.tile_offset = (unsigned long long*)to;
+  sp.bulk0_count = (unsigned long long*)b0;
+  sp.bulk0_rows = src->has_bulks ? (long long)src->bulk0_rows : 0;
+  cudaError_t e = cudaMemsetAsync(b0, 0, 8, x->stream);
+  cudaEvent_t ev;
+  x->prof_begin(SVM_K_SELECT, &ev);
+  if (!e) e = launch_select_count(sp, x->stream);
+  if (!e) e = launch_exclusive_scan(sp.tile_count, tiles, (unsigned long long*)to, (unsigned long long*)tt, x->stream);
+  x->prof_end(SVM_K_SELECT, ev);
+  unsigned long long hdr[2] = {0, 0};
+  if (!e) e = cudaMemcpyAsync(&hdr[0], (unsigned long long*)to + tiles, 8, cudaMemcpyDeviceToHost, x->stream);
+  if (!e) e = cudaMemcpyAsync(&hdr[1], b0, 8, cudaMemcpyDeviceToHost, x->stream);
+  if (e) return x->cuda_fail(e, "select count");
+  if ((st = sync_and_check(x, "select count"))) return st;
+  std::vector<int> types(proj.size(), SVM_INT32);
+  ObjectPtr out = new_result_object(x, b.id, types, hdr[0], &st);
+  if (st) return st;
+  for (int o = 0; o < sp.nout; o++) sp.out[o] = (int32_t*)out->col(o);
+  x->prof_begin(SVM_K_SELECT, &ev);
+  e = launch_select_write(sp, x->stream);
+  x->prof_end(SVM_K_SELECT, ev);
+  if (e) return x->cuda_fail(e, "select write");
+  if ((st = sync_and_check(x, "select write"))) return st;
+  // Output bulk i holds the rows of source bulk i (core/pipeline.cu:161-162, 289-332).
+  out->has_bulks = src->has_bulks;
+  out->bulk0_rows = hdr[1];
+  out->source_rows = src->nrows;
+  x->objects[b.id] = out;
+  return SVM_OK;
+}
+
+// ============================================================ dimension tables
+svm_status build_dim(Ctx* x, const ObjectPtr& obj, int key_col, const std::vector<int>& pay_cols,
+                     DimTablePtr* out) {
+  const bool compat = x->cfg.join_mode == SVM_JOIN_REF_COMPAT;
+  const unsigned ht = (unsigned)(kHashRate * x->cfg.tuple_per_bulk);
+  std::string key = obj->id + "#" + std::to_string(obj->version) + "#" + std::to_string(key_col) + "#";
+  for (int c : pay_cols) key += std::to_string(c) + ",";
+  key += compat ? "#ref" + std::to_string(ht) + (x->cfg.hash_char_signed ? "s" : "u") : "#exact";
+  auto it = x->dim_cache.find(key);
+  if (it != x->dim_cache.end()) {
+    *out = it->second;
+    return SVM_OK;
+  }
+  if (obj->types[key_col] != SVM_INT32) return x->fail(SVM_E_UNSUPPORTED, "join keys must be int32 columns");
+  for (int c : pay_cols)
+    if (obj->types[c] != SVM_INT32) return x->fail(SVM_E_UNSUPPORTED, "joined columns must be int32");
+  if (pay_cols.size() > (size_t)(kMaxKeys + 2 * kMaxMetrics))
+    return x->fail(SVM_E_UNSUPPORTED, "too many columns of one joined object");
+  // REF_COMPAT: only bulk 0 of the joined object is probed (core/pipeline.cu:91, 295).
+  long long n = compat ? (obj->has_bulks ? (long long)obj->bulk0_rows : 0) : (long long)obj->nrows;
+  auto T = std::make_shared<DimTable>();
+  T->rows_considered = (unsigned long long)n;
+  T->pay_cols = pay_cols;
+
+  BuildInput in{};
+  in.key = (const int32_t*)obj->col(key_col);
+  in.n = n;
+  in.npay = (int)pay_cols.size();
+  for (size_t f = 0; f < pay_cols.size(); f++) in.pay[f] = (const int32_t*)obj->col(pay_cols[f]);
+
+  x->scratch_reset();
+  size_t rc = compat && n > 0 ? refcompat_scratch_bytes(n, ht) : 0;
+  size_t stats_words = 2 + 2 * pay_cols.size() + 1;
+  svm_status st = x->scratch_reserve(rc + 4 * stats_words + 4096);
+  if (st) return st;
+  void *rcs = nullptr, *stats = nullptr;
+  DevBufPtr dropped;  // REF_COMPAT: rows the reference's table leaves out
+  if (rc && ((st = x->alloc((size_t)n, &dropped)) || (st = x->scratch_take(rc, &rcs)))) return st;
+  if ((st = x->scratch_take(4 * stats_words, &stats))) return st;
+  cudaError_t e = cudaSuccess;
+  cudaEvent_t ev;
+  x->prof_begin(SVM_K_BUILD, &ev);
+  if (rc) {
+    e = launch_refcompat(in.key, n, ht, x->cfg.hash_char_signed, (uint8_t*)dropped->p, rcs, x->stream);
+    in.dropped = (const uint8_t*)dropped->p;
+  }
+  std::vector<int32_t> hs(stats_words);
+  for (size_t f = 0; f < stats_words - 1; f += 2) {
+    hs[f] = INT_MAX;
+    hs[f + 1] = INT_MIN;
+  }
+  hs[stats_words - 1] = 0;
+  if (!e) e = cudaMemcpyAsync(stats, hs.data(), 4 * stats_words, cudaMemcpyHostToDevice, x->stream);
+  if (!e) e = launch_build_stats(in, (int32_t*)stats, x->stream);
+  if (!e) e = cudaMemcpyAsync(hs.data(), stats, 4 * stats_words, cudaMemcpyDeviceToHost, x->stream);
+  x->prof_end(SVM_K_BUILD, ev);
+  if (e) return x->cuda_fail(e, "dimension stats");
+  if ((st = sync_and_check(x, "dimension stats"))) return st;
+  T->live = (uint32_t)hs[stats_words - 1];
+  T->key_min = hs[0];
+  T->key_max = hs[1];
+  for (size_t f = 0; f < pay_cols.size(); f++) {
+    T->pay_min.push_back(hs[2 + 2 * f]);
+    T->pay_max.push_back(hs[3 + 2 * f]);
+  }
+
+  DimDesc& d = T->desc;
+  d.smem_word_off = -1;
+  d.npay = (int)pay_cols.size();
+  if (T->live == 0) {
+    // Nothing joinable: a dense table with an empty key range.
+    d.layout = LAYOUT_DENSE;
+    d.entry_bits = 1;
+    d.key_min = 0;
+    d.span = 0;
+    d.table_words = 1;
+    if ((st = x->alloc(4, &T->words, true))) return st;
+    d.words = (const uint32_t*)T->words->p;
+    for (int f = 0; f < d.npay; f++) d.pay[f] = PayloadField{nullptr, 0, 1, 0};
+    x->dim_cache[key] = T;
+    *out = T;
+    return SVM_OK;
+  }
+  // Payload: bit-pack each column as (value - min) when the entry fits 32
+  // bits, else store the row index and gather the columns at probe time.
+  int bits_total = 1;
+  std::vector<int> fbits(pay_cols.size());
+  for (size_t f = 0; f < pay_cols.size(); f++) {
+    unsigned long long range = (unsigned long long)((long long)T->pay_max[f] - T->pay_min[f] + 1);
+    fbits[f] = ceil_log2(range);
+    bits_total += fbits[f];
+  }
+  bool row_index = bits_total > 32;
+  if (row_index) {
+    int rb = ceil_log2((unsigned long long)n);
+    bits_total = 1 + rb;
+    for (size_t f = 0; f < pay_cols.size(); f++)
+      d.pay[f] = PayloadField{(const int32_t*)obj->col(pay_cols[f]), 0, 1, (uint8_t)rb};
+  } else {
+    int shift = 1;
+    for (size_t f = 0; f < pay_cols.size(); f++) {
+      d.pay[f] = PayloadField{nullptr, T->pay_min[f], (uint8_t)shift, (uint8_t)fbits[f]};
+      shift += fbits[f];
+    }
+  }
+  int entry_bits = 1;
+  while (entry_bits < bits_total) entry_bits <<= 1;
+  unsigned long long span = (unsigned long long)((long long)T->key_max - T->key_min + 1);
+  unsigned long long cap = 16;
+  while (cap < 2 * T->live) cap <<= 1;
+  unsigned long long dense_bytes = (span * entry_bits + 31) / 32 * 4;
+  unsigned long long hash_bytes = cap * 8;
+  bool dense = span <= (1ull << 32) - 1 && dense_bytes <= std::max(2 * hash_bytes, 64ull << 10);
+  d.key_min = T->key_min;
+  x->scratch_reset();
+  if (dense) {
+    d.layout = LAYOUT_DENSE;
+    d.entry_bits = entry_bits;
+    d.span = (uint32_t)span;
+    d.table_words = (uint32_t)(dense_bytes / 4);
+    if ((st = x->alloc(dense_bytes, &T->words))) return st;
+    d.words = (const uint32_t*)T->words->p;
+    void* owner;
+    if ((st = x->scratch_reserve(4 * span + 256)) || (st = x->scratch_take(4 * span, &owner))) return st;
+    x->prof_begin(SVM_K_BUILD, &ev);
+    e = launch_build_dense(in, d, (int32_t*)owner, (uint32_t*)T->words->p, x->stream);
+    x->prof_end(SVM_K_BUILD, ev);
+  } else {
+    if (bits_total > 32) return x->fail(SVM_E_UNSUPPORTED, "joined payload too wide");
+    d.layout = LAYOUT_HASH;
+    d.entry_bits = 32;
+    d.span = (uint32_t)cap;
+    d.table_words = (uint32_t)(2 * cap);
+    if ((st = x->alloc(hash_bytes, &T->words))) return st;
+    d.words = (const uint32_t*)T->words->p;
+    void* slots;
+    size_t need = 8 * cap + 256;
+    if ((st = x->scratch_reserve(need)) || (st = x->scratch_take(8 * cap, &slots))) return st;
+    x->prof_begin(SVM_K_BUILD, &ev);
+    e = launch_build_hash(in, d, (unsigned long long*)slots, (uint32_t*)T->words->p, x->d_error, x->stream);
+    x->prof_end(SVM_K_BUILD, ev);
+  }
+  if (e) return x->cuda_fail(e, "dimension build");
+  if ((st = sync_and_check(x, "dimension build"))) return st;
+  x->dim_cache[key] = T;
+  *out = T;
+  return SVM_OK;
+}
+
+// ============================================================ star queries
+struct StepPlan {
+  Step step;
+  double est;      // fraction of rows expected to survive the step
+  int order_class; // 0 filter/probe, 1 plain load
+};
+
+svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs) {
+  std::string err;
+  const int nkeys = (int)b.reduce_key.size();
+  const int nmet = (int)b.metric_exp.size();
+  if (nkeys > kMaxKeys) return x->fail(SVM_E_UNSUPPORTED, "more than 3 ReduceBy dims (as the reference)");
+  if (nmet < 1 || nmet > kMaxMetrics) return x->fail(SVM_E_UNSUPPORTED, "ReduceBy needs 1..3 metrics");
+  if ((int)b.sink.size() < nkeys + nmet)
+    return x->fail(SVM_E_INVALID_ARG, "Sink schema has fewer columns than dims + metrics");
+  int wide[kMaxMetrics];
+  for (int m = 0; m < nmet; m++) {
+    int t = b.sink[nkeys + m].type;
+    if (t != SVM_INT64 && t != SVM_INT32)
+      return x->fail(SVM_E_UNSUPPORTED, "metric columns must be declared Int32 or Int64");
+    wide[m] = t == SVM_INT64;
+  }
+  // ---- joins: object k (1..n) is joined at most once, on a fact column.
+  const int nref = (int)refs.size();
+  if (nref > kMaxDims) return x->fail(SVM_E_UNSUPPORTED, "more than 4 joined objects");
+  std::vector<int> join_of_obj(nref + 1, -1);
+  for (size_t j = 0; j < b.join_rkey.size(); j++) {
+    ColRef l = b.join_lkey[j], r = b.join_rkey[j];
+    if (r.obj < 1 || r.obj > nref) return x->fail(SVM_E_INVALID_ARG, "rkey names an object the pipeline does not list");
+    if (l.obj != 0) return x->fail(SVM_E_UNSUPPORTED, "lkey must be a column of the source object");
+    if (join_of_obj[r.obj] >= 0) return x->fail(SVM_E_UNSUPPORTED, "an object joined twice");
+    if (l.col < 0 || l.col >= src->ncols || r.col < 0 || r.col >= refs[r.obj - 1]->ncols)
+      return x->fail(SVM_E_INVALID_ARG, "join column out of range");
+    if (src->types[l.col] != SVM_INT32) return x->fail(SVM_E_UNSUPPORTED, "join keys must be int32");
+    join_of_obj[r.obj] = (int)j;
+  }
+  // ---- expressions
+  Expr pred;
+  bool has_pred = !b.filter_exp.empty();
+  if (has_pred) {
+    std::string t = join_filters(b.filter_exp);
+    if (!parse_expr(t, &pred, &err))
+      return x->fail(err.rfind("unsupported", 0) == 0 ? SVM_E_UNSUPPORTED : SVM_E_INVALID_ARG,
+                     "predication '" + t + "': " + err);
+  }
+  std::vector<Expr> mexp(nmet);
+  for (int m = 0; m < nmet; m++)
+    if (!parse_expr(b.metric_exp[m], &mexp[m], &err))
+      return x->fail(err.rfind("unsupported", 0) == 0 ? SVM_E_UNSUPPORTED : SVM_E_INVALID_ARG,
+                     "metric '" + b.metric_exp[m] + "': " + err);
+  auto check_ref = [&](const ColRef& r, bool allow_dims) -> svm_status {
+    if (r.obj == 0) {
+      if (r.col < 0 || r.col >= src->ncols) return x->fail(SVM_E_INVALID_ARG, "column out of range");
+      if (src->types[r.col] != SVM_INT32) return x->fail(SVM_E_UNSUPPORTED, "only int32 fact columns");
+      return SVM_OK;
+    }
+    if (!allow_dims)
+      return x->fail(SVM_E_UNSUPPORTED, "a Filter on a joined object (the reference evaluates filters before joins)");
+    if (r.obj > nref || join_of_obj[r.obj] < 0)
+      return x->fail(SVM_E_INVALID_ARG, "reference to object " + std::to_string(r.obj) + " that is not joined");
+    if (r.col < 0 || r.col >= refs[r.obj - 1]->ncols) return x->fail(SVM_E_INVALID_ARG, "column out of range");
+    return SVM_OK;
+  };
+  std::vector<ColRef> pred_refs, met_refs;
+  if (has_pred) collect_refs(pred, pred.root, &pred_refs);
+  for (auto& r : pred_refs)
+    if (svm_status s = check_ref(r, false)) return s;
+  for (int m = 0; m < nmet; m++) collect_refs(mexp[m], mexp[m].root, &met_refs);
+  for (auto& r : met_refs)
+    if (svm_status s = check_ref(r, true)) return s;
+  for (auto& r : b.reduce_key)
+    if (svm_status s = check_ref(r, true)) return s;
+
+  // ---- the result object's shape
+  std::vector<int> out_types(nkeys, SVM_INT32);
+  for (int m = 0; m < nmet; m++) out_types.push_back(wide[m] ? SVM_INT64 : SVM_INT32);
+  svm_status st;
+  if (!src->has_bulks) {
+    // No fact bulks: the reference runs no task and its sink stays empty.
+    ObjectPtr out = new_result_object(x, b.id, out_types, 0, &st);
+    if (st) return st;
+    x->objects[b.id] = out;
+    return SVM_OK;
+  }
+
+  // ---- filter conjuncts: ranges per fact column, the rest residual
+  std::map<int, std::pair<int32_t, int32_t>> ranges;
+  bool empty = false;
+  std::vector<int> residual;
+  if (has_pred) {
+    std::vector<int> conj;
+    flatten_and(pred, pred.root, &conj);
+    for (int c : conj) {
+      ColRef r;
+      int32_t lo, hi, v;
+      if (as_range(pred, c, &r, &lo, &hi)) {
+        auto it = ranges.find(r.col);
+        if (it == ranges.end()) {
+          ranges[r.col] = {lo, hi};
+        } else {
+          it->second.first = std::max(it->second.first, lo);
+          it->second.second = std::min(it->second.second, hi);
+        }
+        if (lo > hi) empty = true;
+      } else if (const_value(pred, c, &v)) {
+        if (!v) empty = true;
+      } else {
+        residual.push_back(c);
+      }
+    }
+    for (auto& kv : ranges)
+      if (kv.second.first > kv.second.second) empty = true;
+  }
+
+  // ---- dimension tables: payload = the joined object's columns used by keys/metrics
+  std::vector<std::vector<int>> pay(nref + 1);
+  auto add_pay = [&](const ColRef& r) {
+    if (r.obj == 0) return;
+    auto& v = pay[r.obj];
+    if (std::find(v.begin(), v.end(), r.col) == v.end()) v.push_back(r.col);
+  };
+  for (auto& r : met_refs) add_pay(r);
+  for (auto& r : b.reduce_key) add_pay(r);
+  std::vector<DimTablePtr> tables(nref + 1);
+  for (int k = 1; k <= nref; k++) {
+    if (join_of_obj[k] < 0) continue;
+    std::sort(pay[k].begin(), pay[k].end());
+    st = build_dim(x, refs[k - 1], b.join_rkey[join_of_obj[k]].col, pay[k], &tables[k]);
+    if (st) return st;
+  }
+
+  // ---- steps
+  StarParams P{};
+  P.error = x->d_error;
+  P.row_begin = (long long)src->row0;
+  P.row_end = (long long)(src->row0 + src->nrows);
+  std::vector<int> fact_cols;  // distinct fact columns -> StarParams::cols index
+  auto col_index = [&](int c) {
+    for (size_t i = 0; i < fact_cols.size(); i++)
+      if (fact_cols[i] == c) return (int)i;
+    fact_cols.push_back(c);
+    return (int)fact_cols.size() - 1;
+  };
+  std::vector<StepPlan> plan;
+  std::vector<int> dim_of_obj(nref + 1, -1);
+  int ndims = 0;
+  // Probe steps (with any range on the same fact column folded in).
+  std::set<int> ranged_done;
+  for (int k = 1; k <= nref; k++) {
+    if (join_of_obj[k] < 0) continue;
+    int lc = b.join_lkey[join_of_obj[k]].col;
+    StepPlan sp{};
+    sp.step.kind = STEP_PROBE;
+    sp.step.col = col_index(lc);
+    sp.step.lo = INT_MIN;
+    sp.step.hi = INT_MAX;
+    sp.step.dim = ndims;
+    dim_of_obj[k] = ndims++;
+    const DimTablePtr& T = tables[k];
+    unsigned long long base_rows = std::max<unsigned long long>(1, refs[k - 1]->source_rows);
+    sp.est = std::min(1.0, (double)T->live / (double)base_rows);
+    auto r = ranges.find(lc);
+    if (r != ranges.end() && !ranged_done.count(lc)) {
+      sp.step.lo = r->second.first;
+      sp.step.hi = r->second.second;
+      ranged_done.insert(lc);
+      ColStats cs;
+      if ((st = x->column_stats(src, lc, &cs))) return st;
+      double w = (double)cs.max - cs.min + 1;
+      double ov = std::max(0.0, (double)std::min(cs.max, r->second.second) - std::max(cs.min, r->second.first) + 1);
+      sp.est *= ov / w;
+    }
+    sp.order_class = 0;
+    plan.push_back(sp);
+  }
+  for (auto& kv : ranges) {
+    if (ranged_done.count(kv.first)) continue;
+    StepPlan sp{};
+    sp.step.kind = STEP_RANGE;
+    sp.step.col = col_index(kv.first);
+    sp.step.lo = kv.second.first;
+    sp.step.hi = kv.second.second;
+    ColStats cs;
+    if ((st = x->column_stats(src, kv.first, &cs))) return st;
+    double w = (double)cs.max - cs.min + 1;
+    double ov = std::max(0.0, (double)std::min(cs.max, kv.second.second) - std::max(cs.min, kv.second.first) + 1);
+    sp.est = ov / w;
+    sp.order_class = 0;
+    plan.push_back(sp);
+  }
+  std::stable_sort(plan.begin(), plan.end(), [](const StepPlan& a, const StepPlan& z) {
+    if (a.order_class != z.order_class) return a.order_class < z.order_class;
+    return a.est < z.est;
+  });
+  // Operands: fact columns read raw need a step whose slot keeps the raw
+  // value (a RANGE step does; a PROBE step replaces it with the entry).
+  std::vector<ColRef> all_refs = met_refs;
+  for (auto& r : b.reduce_key)
+    if (std::find(all_refs.begin(), all_refs.end(), r) == all_refs.end()) all_refs.push_back(r);
+  std::vector<ColRef> resid_refs;
+  for (int c : residual) collect_refs(pred, c, &resid_refs);
+  for (auto& r : resid_refs)
+    if (std::find(all_refs.begin(), all_refs.end(), r) == all_refs.end()) all_refs.push_back(r);
+  auto raw_slot = [&](int fact_col) -> int {
+    for (size_t s = 0; s < plan.size(); s++)
+      if (plan[s].step.kind != STEP_PROBE && fact_cols[plan[s].step.col] == fact_col) return (int)s;
+    return -1;
+  };
+  for (auto& r : all_refs) {
+    if (r.obj != 0 || raw_slot(r.col) >= 0) continue;
+    StepPlan sp{};
+    sp.step.kind = STEP_LOAD;
+    sp.step.col = col_index(r.col);
+    sp.step.lo = INT_MIN;
+    sp.step.hi = INT_MAX;
+    sp.est = 1.0;
+    sp.order_class = 1;
+    plan.push_back(sp);
+  }
+  if ((int)plan.size() > kMaxSteps || (int)fact_cols.size() > kMaxSteps)
+    return x->fail(SVM_E_UNSUPPORTED, "query touches more than 8 fact columns");
+  P.nsteps = (int)plan.size();
+  for (size_t s = 0; s < plan.size(); s++) P.steps[s] = plan[s].step;
+  for (size_t i = 0; i < fact_cols.size(); i++) P.cols[i] = (const int32_t*)src->base(fact_cols[i]);
+  auto operand_of = [&](const ColRef& r, Operand* o) -> bool {
+    if (r.obj == 0) {
+      int s = raw_slot(r.col);
+      if (s < 0) return false;
+      *o = Operand{(int8_t)s, -1};
+      return true;
+    }
+    int d = dim_of_obj[r.obj];
+    for (int s = 0; s < P.nsteps; s++)
+      if (P.steps[s].kind == STEP_PROBE && P.steps[s].dim == d) {
+        auto& pv = pay[r.obj];
+        int f = (int)(std::find(pv.begin(), pv.end(), r.col) - pv.begin());
+        *o = Operand{(int8_t)s, (int8_t)f};
+        return true;
+      }
+    return false;
+  };
+  // ---- dims into StarParams, small ones staged in shared memory
+  P.ndims = ndims;
+  std::vector<std::pair<size_t, int>> by_size;
+  for (int k = 1; k <= nref; k++) {
+    if (dim_of_obj[k] < 0) continue;
+    P.dims[dim_of_obj[k]] = tables[k]->desc;
+    P.dims[dim_of_obj[k]].smem_word_off = -1;
+    by_size.push_back({(size_t)tables[k]->desc.table_words * 4, dim_of_obj[k]});
+  }
+  std::sort(by_size.begin(), by_size.end());
+  int smem_words = 0;
+  for (auto& bs : by_size) {
+    if ((size_t)smem_words * 4 + bs.first > (size_t)kSmemTableBytes) break;
+    P.dims[bs.second].smem_word_off = smem_words;
+    smem_words += (int)((bs.first / 4 + 3) & ~size_t(3));
+  }
+  P.smem_table_words = smem_words;
+  // ---- operand table for bytecode programs
+  std::vector<ColRef> prog_refs;
+  auto add_prog_refs = [&](const Expr& e, int node) { collect_refs(e, node, &prog_refs); };
+  for (int c : residual) add_prog_refs(pred, c);
+  for (int m = 0; m < nmet; m++) add_prog_refs(mexp[m], mexp[m].root);
+  if (prog_refs.size() > 16) return x->fail(SVM_E_UNSUPPORTED, "more than 16 columns in expressions");
+  P.nopnd = (int)prog_refs.size();
+  for (size_t i = 0; i < prog_refs.size(); i++)
+    if (!operand_of(prog_refs[i], &P.opnds[i])) return x->fail(SVM_E_INVALID_ARG, "internal: unbound operand");
+  if (residual.size() > (size_t)kMaxPost) return x->fail(SVM_E_UNSUPPORTED, "too many non-range filter terms");
+  P.npost = (int)residual.size();
+  for (size_t i = 0; i < residual.size(); i++)
+    if (!compile_prog(pred, residual[i], prog_refs, &P.post[i], &err)) return x->fail(SVM_E_UNSUPPORTED, err);
+  // ---- metrics
+  P.nmetrics = nmet;
+  for (int m = 0; m < nmet; m++) {
+    Metric& M = P.metrics[m];
+    const Node& root = mexp[m].nodes[mexp[m].root];
+    if (root.kind == N_COL && operand_of(root.ref, &M.a)) {
+      M.form = MF_OPND;
+    } else if (root.kind == N_BINARY && (root.op == X_ADD || root.op == X_SUB || root.op == X_MUL) &&
+               mexp[m].nodes[root.a].kind == N_COL && mexp[m].nodes[root.b].kind == N_COL &&
+               operand_of(mexp[m].nodes[root.a].ref, &M.a) && operand_of(mexp[m].nodes[root.b].ref, &M.b)) {
+      M.form = root.op == X_ADD ? MF_ADD : root.op == X_SUB ? MF_SUB : MF_MUL;
+    } else {
+      M.form = MF_PROG;
+      if (!compile_prog(mexp[m], mexp[m].root, prog_refs, &M.prog, &err)) return x->fail(SVM_E_UNSUPPORTED, err);
+    }
+  }
+  // ---- keys and the aggregation layout
+  P.nkeys = nkeys;
+  unsigned long long G = 1;
+  for (int q = 0; q < nkeys; q++) {
+    const ColRef& r = b.reduce_key[q];
+    if (!operand_of(r, &P.keys[q])) return x->fail(SVM_E_INVALID_ARG, "internal: unbound key");
+    int32_t lo, hi;
+    if (r.obj == 0) {
+      ColStats cs;
+      if ((st = x->column_stats(src, r.col, &cs))) return st;
+      lo = cs.min;
+      hi = cs.max;
+    } else {
+      const DimTablePtr& T = tables[r.obj];
+      auto& pv = pay[r.obj];
+      int f = (int)(std::find(pv.begin(), pv.end(), r.col) - pv.begin());
+      lo = T->live ? T->pay_min[f] : 0;
+      hi = T->live ? T->pay_max[f] : 0;
+    }
+    if (hi < lo) hi = lo;
+    P.kmin[q] = lo;
+    P.krange[q] = (uint32_t)std::min<long long>((long long)hi - lo + 1, 0xFFFFFFFFll);
+    if ((long long)hi - lo + 1 > (1ll << 26) || G * P.krange[q] > (1ull << 26))
+      return x->fail(SVM_E_UNSUPPORTED, "group-key space above 2^26 groups (hash aggregation not built)");
+    G *= P.krange[q];
+  }
+  unsigned long long stride = 1;
+  for (int q = nkeys - 1; q >= 0; q--) {
+    P.kstride[q] = stride;
+    stride *= P.krange[q];
+  }
+  P.ngroups = G;
+  if (nkeys == 0)
+    P.agg = AGG_SCALAR;
+  else if (G * (8ull * nmet + 4) <= (unsigned long long)kSmemAggBytes)
+    P.agg = AGG_DENSE_SMEM;
+  else
+    P.agg = AGG_DENSE_GLOBAL;
+
+  // ---- scratch: sums + counts (+ finalize buffers)
+  x->scratch_reset();
+  size_t agg_bytes = 8 * (size_t)G * (nmet + 1);
+  size_t fin_bytes = nkeys ? 8 * ((G + 1) / 2 + 1 + G + 1) + 8 * scan_tmp_words(G) : 0;
+  if ((st = x->scratch_reserve(agg_bytes + fin_bytes + 4096))) return st;
+  void *sums, *fin = nullptr, *scant = nullptr;
+  if ((st = x->scratch_take(agg_bytes, &sums))) return st;
+  if (nkeys && ((st = x->scratch_take(8 * ((G + 1) / 2 + 1 + G + 1), &fin)) ||
+                (st = x->scratch_take(8 * scan_tmp_words(G), &scant))))
+    return st;
+  P.sums = (unsigned long long*)sums;
+  P.counts = P.sums + (size_t)nmet * G;
+  cudaError_t e = cudaMemsetAsync(sums, 0, agg_bytes, x->stream);
+  if (e) return x->cuda_fail(e, "cudaMemsetAsync");
+  if (empty) P.row_end = P.row_begin;  // a contradictory filter: no row can pass
+
+  size_t smem = star_smem_bytes(P);
+  if (smem > 200 * 1024) return x->fail(SVM_E_UNSUPPORTED, "shared-memory plan too large");
+  int grid = star_grid_size(P, smem);
+  cudaEvent_t ev;
+  x->prof_begin(SVM_K_STAR, &ev);
+  e = launch_star(P, grid, star_block_size(), smem, x->stream);
+  x->prof_end(SVM_K_STAR, ev);
+  if (e) return x->cuda_fail(e, "star kernel");
+
+  ObjectPtr out;
+  if (nkeys == 0) {
+    std::vector<unsigned long long> h(nmet);
+    e = cudaMemcpyAsync(h.data(), sums, 8 * nmet, cudaMemcpyDeviceToHost, x->stream);
+    if (e) return x->cuda_fail(e, "result copy");
+    if ((st = sync_and_check(x, "star query"))) return st;
+    out = new_result_object(x, b.id, out_types, 1, &st);
+    if (st) return st;
+    for (int m = 0; m < nmet; m++) {
+      if (wide[m]) {
+        long long v = (long long)h[m];
+        e = cudaMemcpyAsync(out->col(m), &v, 8, cudaMemcpyHostToDevice, x->stream);
+      } else {
+        int32_t v = (int32_t)(uint32_t)h[m];
+        e = cudaMemcpyAsync(out->col(m), &v, 4, cudaMemcpyHostToDevice, x->stream);
+      }
+      if (!e) e = cudaStreamSynchronize(x->stream);
+      if (e) return x->cuda_fail(e, "result store");
+    }
+  } else {
+    x->prof_begin(SVM_K_FINALIZE, &ev);
+    e = launch_finalize_dense(P, nullptr, nullptr, nullptr, (unsigned long long*)fin,
+                              (unsigned long long*)scant, nullptr, x->stream);
+    x->prof_end(SVM_K_FINALIZE, ev);
+    unsigned long long ng = 0;
+    unsigned long long* pos = (unsigned long long*)fin + (G + 1) / 2 + 1;
+    if (!e) e = cudaMemcpyAsync(&ng, pos + G, 8, cudaMemcpyDeviceToHost, x->stream);
+    if (e) return x->cuda_fail(e, "finalize");
+    if ((st = sync_and_check(x, "star query"))) return st;
+    out = new_result_object(x, b.id, out_types, ng, &st);
+    if (st) return st;
+    int32_t* kout[kMaxKeys];
+    void* mout[kMaxMetrics];
+    for (int q = 0; q < nkeys; q++) kout[q] = (int32_t*)out->col(q);
+    for (int m = 0; m < nmet; m++) mout[m] = out->col(nkeys + m);
+    x->prof_begin(SVM_K_FINALIZE, &ev);
+    e = launch_finalize_dense(P, kout, mout, wide, (unsigned long long*)fin, (unsigned long long*)scant,
+                              nullptr, x->stream);
+    x->prof_end(SVM_K_FINALIZE, ev);
+    if (e) return x->cuda_fail(e, "finalize write");
+    if ((st = sync_and_check(x, "finalize"))) return st;
+  }
+  out->has_bulks = true;
+  out->bulk0_rows = out->nrows;
+  x->objects[b.id] = out;
+  return SVM_OK;
+}
+
+}  // namespace
+
+svm_status run_pipeline(Ctx* x, const svm_pipeline* p) {
+  Bound b;
+  svm_status st = bind(x, p, &b);
+  if (st) return st;
+  if (p->npre < 1 || !p->pre_pipeline_id || !p->pre_pipeline_id[0])
+    return x->fail(SVM_E_INVALID_ARG, "pipeline " + b.id + " has no source object (pre_pipeline_id[0])");
+  // service/service.cu:36-49: every pre_pipeline_id must name a cached object.
+  ObjectPtr src = x->find(p->pre_pipeline_id[0]);
+  if (!src) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + p->pre_pipeline_id[0]);
+  std::vector<ObjectPtr> refs;
+  for (int i = 1; i < p->npre; i++) {
+    ObjectPtr o = p->pre_pipeline_id[i] ? x->find(p->pre_pipeline_id[i]) : nullptr;
+    if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + (p->pre_pipeline_id[i] ? p->pre_pipeline_id[i] : "(null)"));
+    refs.push_back(o);
+  }
+  if (!b.is_reduce) return run_select(x, b, src);
+  return run_star(x, b, src, refs);
+}
+
+svm_status run_batch(Ctx* x, int n, const svm_pipeline* p) {
+  for (int i = 0; i < n; i++) {
+    svm_status st = run_pipeline(x, &p[i]);
+    if (st) return st;
+  }
+  return SVM_OK;
+}
+
+}  // namespace svm

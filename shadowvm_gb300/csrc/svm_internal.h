@@ -1,0 +1,147 @@
+// Internal definitions shared by the host planner (C++) and the kernels (CUDA).
+// Everything that crosses into a kernel is a plain struct passed by value.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace svm {
+
+// ---------------------------------------------------------------- limits
+constexpr int kMaxSteps = 8;       // fact columns one fused scan touches
+constexpr int kMaxDims = 4;        // joined objects per query (join_index[8] in the reference)
+constexpr int kMaxKeys = 3;        // ReduceTask handles 0..3 keys (core/pipeline.cu:373-471)
+constexpr int kMaxMetrics = 3;     // ... and 1..3 metrics
+constexpr int kMaxProg = 48;       // bytecode ops per expression
+constexpr int kMaxPost = 4;        // residual predicates evaluated after the steps
+constexpr int kSmemTableBytes = 64 * 1024;  // dimension tables staged in shared memory per block
+constexpr int kSmemAggBytes = 64 * 1024;    // per-block group table in shared memory
+constexpr int kHashRate = 5;       // com/cpp/define.hpp:29
+
+// ---------------------------------------------------------------- expressions
+// Stack-machine bytecode for int32 C expressions (wrapping arithmetic, C
+// truncating division, comparisons yield 0/1, && || short-circuit).
+enum ExprOp : uint8_t {
+  X_OPND = 0,   // push operand[arg]
+  X_CONST,      // push constant[arg]
+  X_NEG, X_NOT, X_BNOT,
+  X_ADD, X_SUB, X_MUL, X_DIV, X_MOD, X_SHL, X_SHR,
+  X_LT, X_LE, X_GT, X_GE, X_EQ, X_NE, X_BAND, X_BXOR, X_BOR,
+  X_NORM,       // top = (top != 0)
+  X_JZ_KEEP,    // if top == 0: jump to arg (keep the 0) else pop
+  X_JNZ_ONE,    // if top != 0: top = 1, jump to arg; else pop
+  X_JZ_POP,     // pop; if it was 0 jump to arg
+  X_JMP,
+};
+
+struct Prog {
+  uint8_t n;                 // ops
+  uint8_t op[kMaxProg];
+  uint8_t arg[kMaxProg];
+  int32_t konst[16];
+};
+
+// Operand reference: either a fact column value held in step slot `slot`, or
+// a payload field of the dimension probed in step slot `slot`.
+struct Operand {
+  int8_t slot;     // step index holding the fact value / payload word
+  int8_t field;    // -1: the fact value itself; >= 0: payload field index
+};
+
+// ---------------------------------------------------------------- dimension tables
+enum TableLayout : int { LAYOUT_DENSE = 0, LAYOUT_HASH = 1 };
+
+// A built dimension table.  DENSE: entry for key k at bit offset
+// (k - key_min) * entry_bits of `words`; bit 0 of the entry is "present",
+// payload fields follow.  HASH: `cap` slots of {int key, uint32 payload word}
+// (payload word bit 0 = present), linear probing from mix32(key) & (cap - 1).
+struct PayloadField {
+  const int32_t* col;  // non-null: value = col[(entry >> shift) & mask] (row-index payload)
+  int32_t min;         // else:     value = min + ((entry >> shift) & mask)
+  uint8_t shift;
+  uint8_t bits;
+};
+
+struct DimDesc {
+  int layout;
+  const uint32_t* words;     // global table
+  int smem_word_off;         // >= 0: staged into shared memory at this word offset
+  int entry_bits;            // DENSE: 1,2,4,8,16,32
+  int32_t key_min;
+  uint32_t span;             // DENSE: key range; HASH: capacity (power of two)
+  uint32_t table_words;      // 32-bit words
+  int npay;
+  PayloadField pay[kMaxKeys + 2 * kMaxMetrics];
+};
+
+__host__ __device__ inline uint32_t mix32(uint32_t x) {
+  // murmur3 fmix32 (Appleby, public domain)
+  x ^= x >> 16; x *= 0x85ebca6bu; x ^= x >> 13; x *= 0xc2b2ae35u; x ^= x >> 16;
+  return x;
+}
+
+// ---------------------------------------------------------------- fused star query
+enum StepKind : int { STEP_RANGE = 0, STEP_PROBE = 1, STEP_LOAD = 2 };
+
+struct Step {
+  int kind;
+  int col;          // fact column index into StarParams::cols
+  int32_t lo, hi;   // STEP_RANGE: keep lo <= v <= hi
+  int dim;          // STEP_PROBE
+};
+
+enum MetricForm : int { MF_OPND = 0, MF_ADD = 1, MF_SUB = 2, MF_MUL = 3, MF_PROG = 4 };
+
+struct Metric {
+  int form;
+  Operand a, b;     // MF_OPND uses a; binary forms use a (op) b
+  Prog prog;        // MF_PROG: operands index StarParams::opnds
+};
+
+enum AggMode : int { AGG_SCALAR = 0, AGG_DENSE_SMEM = 1, AGG_DENSE_GLOBAL = 2, AGG_HASH_GLOBAL = 3 };
+
+struct StarParams {
+  const int32_t* cols[kMaxSteps];   // fact column base pointers (row 0 of the base allocation)
+  long long row_begin, row_end;     // rows [row_begin, row_end) of the base columns
+  int nsteps;
+  Step steps[kMaxSteps];
+  int ndims;
+  DimDesc dims[kMaxDims];
+  int npost;                        // residual predicates (bytecode over opnds)
+  Prog post[kMaxPost];
+  int nopnd;
+  Operand opnds[16];                // operand table for bytecode programs
+  int nkeys;
+  Operand keys[kMaxKeys];
+  int32_t kmin[kMaxKeys];
+  uint32_t krange[kMaxKeys];
+  unsigned long long kstride[kMaxKeys];
+  int nmetrics;
+  Metric metrics[kMaxMetrics];
+  int agg;
+  unsigned long long ngroups;       // dense: product of ranges; hash: capacity
+  unsigned long long* sums;         // [nmetrics][ngroups] int64 (two's complement)
+  unsigned long long* counts;       // [ngroups]
+  unsigned long long* hkeys;        // AGG_HASH_GLOBAL: packed keys per slot (~0 = empty)
+  int smem_table_words;             // words of dimension tables staged in shared memory
+  int* error;                       // device error word (division by zero, hash overflow)
+};
+
+// ---------------------------------------------------------------- select (Map) pipelines
+struct SelectParams {
+  const int32_t* cols[16];
+  int ncols_in;
+  long long nrows;
+  int npred;                        // conjunct programs over input columns (operand = column)
+  Prog pred[4];
+  int nout;
+  Prog proj[16];                    // one program per output column
+  int32_t* out[16];
+  const unsigned long long* tile_offset;  // exclusive prefix of per-tile pass counts
+  unsigned int* tile_count;
+  unsigned long long* bulk0_count;  // passing rows among source rows [0, bulk0_rows)
+  long long bulk0_rows;
+  int* error;
+};
+
+}  // namespace svm

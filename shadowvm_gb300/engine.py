@@ -1,0 +1,207 @@
+"""Python host API over the C ABI: a data-plane context (`Engine`), its object
+store, and pipeline execution.  The reference equivalents are the
+ObjectStore / cached_obj map and ShadowVMService::RunPipelineCMD
+(object/store.cpp:49-91, service/service.cu:25-63)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import capi
+from .proto import OpType, PipelineInfo, ValType
+
+
+class Engine:
+    """One data-plane context on one GPU."""
+
+    def __init__(self, device: int = 0, tuple_per_bulk: int = 2_000_000, join_mode: str = "ref_compat",
+                 hbm_budget_bytes: int = 0, hash_char_signed: bool = True):
+        self.lib = capi.load()
+        cfg = capi.svm_config()
+        self.lib.svm_config_default(ctypes.byref(cfg))
+        cfg.device = device
+        cfg.tuple_per_bulk = tuple_per_bulk
+        cfg.join_mode = {"ref_compat": capi.JOIN_REF_COMPAT, "exact": capi.JOIN_EXACT}[join_mode]
+        cfg.hbm_budget_bytes = hbm_budget_bytes
+        cfg.hash_char_signed = int(hash_char_signed)
+        h = ctypes.c_void_p()
+        st = self.lib.svm_init(ctypes.byref(cfg), ctypes.byref(h))
+        if st != capi.OK:
+            raise capi.SvmError(st, "svm_init failed (is a CUDA device visible?)")
+        self.h = h
+        self.tuple_per_bulk = tuple_per_bulk
+        self.join_mode = join_mode
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.svm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ------------------------------------------------------------ plumbing
+    def _check(self, st: int):
+        if st != capi.OK:
+            raise capi.SvmError(st, (self.lib.svm_last_error(self.h) or b"").decode())
+
+    @property
+    def stream(self) -> int:
+        return self.lib.svm_stream(self.h)
+
+    def bytes_in_use(self) -> int:
+        return self.lib.svm_bytes_in_use(self.h)
+
+    # ------------------------------------------------------------ objects
+    def put(self, oid: str, columns, on_device: bool = False, nrows: int | None = None):
+        """Store host arrays (int32/int64 numpy) or device pointers as object `oid`.
+        A None column is left zeroed (int32; pass nrows when every column is None)."""
+        n = len(columns)
+        if on_device:
+            ptrs = [ctypes.c_void_p(int(c[0])) for c in columns]  # (ptr, dtype, nrows)
+            types = [capi_type(c[1]) for c in columns]
+            nrows = int(columns[0][2]) if n else 0
+            keep = None
+        else:
+            keep = [None if c is None else np.ascontiguousarray(c) for c in columns]
+            types = [capi_type(np.int32 if c is None else c.dtype) for c in keep]
+            lens = {len(c) for c in keep if c is not None}
+            if len(lens) > 1:
+                raise ValueError("columns differ in length")
+            nrows = lens.pop() if lens else (nrows or 0)
+            ptrs = [ctypes.c_void_p(None if c is None else c.ctypes.data) for c in keep]
+        t = (ctypes.c_int * n)(*types)
+        pa = (ctypes.c_void_p * n)(*ptrs)
+        self._check(self.lib.svm_object_put(self.h, oid.encode(), n, t, nrows, pa, int(on_device)))
+        del keep
+
+    def create(self, oid: str, ncols: int, nrows: int, dtype=np.int32):
+        t = (ctypes.c_int * ncols)(*([capi_type(np.dtype(dtype))] * ncols))
+        self._check(self.lib.svm_object_put(self.h, oid.encode(), ncols, t, nrows, None, 0))
+
+    def gen_uniform(self, oid: str, col: int, seed: int, stream: int, lo: int, hi: int, lookup=None,
+                    row0: int = 0):
+        """Device-side datagen.uniform(seed, stream, lo, hi, row0, nrows) (optionally
+        mapped through `lookup`)."""
+        lut = None
+        if lookup is not None:
+            arr = np.ascontiguousarray(lookup, dtype=np.int32)
+            assert len(arr) == hi - lo + 1
+            lut = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        self._check(self.lib.svm_object_gen_uniform(self.h, oid.encode(), col, seed & (2**64 - 1),
+                                                    stream, row0, lo, hi, lut))
+
+    def kernel_launches(self) -> int:
+        return self.lib.svm_kernel_launches()
+
+    def view(self, oid: str, base: str, row0: int, nrows: int):
+        self._check(self.lib.svm_object_view(self.h, oid.encode(), base.encode(), row0, nrows))
+
+    def info(self, oid: str) -> tuple[int, int]:
+        nc, nr = ctypes.c_int(), ctypes.c_ulonglong()
+        self._check(self.lib.svm_object_info(self.h, oid.encode(), ctypes.byref(nc), ctypes.byref(nr)))
+        return nc.value, nr.value
+
+    def types(self, oid: str) -> list[int]:
+        nc, _ = self.info(oid)
+        t = (ctypes.c_int * max(nc, 1))()
+        self._check(self.lib.svm_object_types(self.h, oid.encode(), t, nc))
+        return list(t)[:nc]
+
+    def read(self, oid: str, col: int, row0: int = 0, n: int | None = None) -> np.ndarray:
+        _, nr = self.info(oid)
+        n = nr - row0 if n is None else n
+        dt = np.int64 if self.types(oid)[col] == ValType.Int64 else np.int32
+        out = np.empty(n, dt)
+        self._check(self.lib.svm_object_read(self.h, oid.encode(), col, row0, n,
+                                             out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def read_all(self, oid: str) -> list[np.ndarray]:
+        nc, _ = self.info(oid)
+        return [self.read(oid, c) for c in range(nc)]
+
+    def device_ptr(self, oid: str, col: int) -> int:
+        p = ctypes.c_void_p()
+        self._check(self.lib.svm_object_device_ptr(self.h, oid.encode(), col, ctypes.byref(p)))
+        return p.value
+
+    def drop(self, oid: str):
+        self._check(self.lib.svm_object_drop(self.h, oid.encode()))
+
+    # ------------------------------------------------------------ pipelines
+    def run(self, pipe: PipelineInfo):
+        """RunPipelineCMD: the output is stored as object `pipe.id`."""
+        keep = []
+        p = marshal(pipe, keep)
+        self._check(self.lib.svm_run_pipeline(self.h, ctypes.byref(p)))
+
+    def run_batch(self, pipes: list[PipelineInfo]):
+        keep = []
+        arr = (capi.svm_pipeline * max(len(pipes), 1))(*[marshal(p, keep) for p in pipes])
+        self._check(self.lib.svm_run_batch(self.h, len(pipes), arr))
+
+    def result(self, oid: str, key_num: int) -> tuple[np.ndarray, np.ndarray]:
+        """A reduce pipeline's output: keys int32 [g, key_num], sums int64 [g, m]."""
+        cols = self.read_all(oid)
+        g = len(cols[0]) if cols else 0
+        keys = np.stack(cols[:key_num], axis=1).astype(np.int32) if key_num else np.zeros((g, 0), np.int32)
+        mets = np.stack([c.astype(np.int64) for c in cols[key_num:]], axis=1) if len(cols) > key_num else \
+            np.zeros((g, 0), np.int64)
+        return keys, mets
+
+    # ------------------------------------------------------------ profiling
+    def profile(self, on: bool = True):
+        self._check(self.lib.svm_profile_enable(self.h, int(on)))
+
+    def profile_reset(self):
+        self._check(self.lib.svm_profile_reset(self.h))
+
+    def profile_read(self, cls: int) -> tuple[int, float]:
+        n, ms = ctypes.c_ulonglong(), ctypes.c_double()
+        self._check(self.lib.svm_profile_read(self.h, cls, ctypes.byref(n), ctypes.byref(ms)))
+        return n.value, ms.value
+
+
+def capi_type(dtype) -> int:
+    dt = np.dtype(dtype)
+    if dt == np.int32:
+        return int(ValType.Int32)
+    if dt == np.int64:
+        return int(ValType.Int64)
+    raise TypeError(f"unsupported column dtype {dt}")
+
+
+def marshal(pipe: PipelineInfo, keep: list) -> capi.svm_pipeline:
+    """PipelineInfo -> svm_pipeline; `keep` holds the buffers alive."""
+    ops = (capi.svm_operator * max(len(pipe.workflow), 1))()
+    for i, op in enumerate(pipe.workflow):
+        items = sorted(op.args.items())
+        args = (capi.svm_arg * max(len(items), 1))(*[capi.svm_arg(k.encode(), v.encode()) for k, v in items])
+        cols = op.output.column_list if op.output is not None else []
+        out = (capi.svm_column_desc * max(len(cols), 1))(
+            *[capi.svm_column_desc(int(c.type), int(c.val_size)) for c in cols])
+        keep += [args, out]
+        ops[i] = capi.svm_operator(int(op.type), len(items), args, len(cols), out)
+    pre = (ctypes.c_char_p * max(len(pipe.pre_pipeline_id), 1))(*[s.encode() for s in pipe.pre_pipeline_id])
+    keep += [ops, pre]
+    return capi.svm_pipeline(pipe.id.encode(), len(pipe.workflow), ops, len(pipe.pre_pipeline_id), pre)
+
+
+def reduce_shape(pipe: PipelineInfo) -> tuple[int, int]:
+    """(key_num, metric_num) of a ReduceBy pipeline, split as the reference does."""
+    from .pipeline import str_split
+    for op in pipe.workflow:
+        if op.type == OpType.ReduceBy:
+            return len(str_split(op.args.get("dim", ""), ",")), len(str_split(op.args["metric"], ","))
+    return 0, 0
