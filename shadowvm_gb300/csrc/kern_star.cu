@@ -1,19 +1,28 @@
 // The fused fact-table scan: range filters and dimension probes in the order
-// the planner chose (most selective first), then group keys and metrics of
-// the surviving rows aggregated per block (registers or shared memory) and
-// merged into int64 group slots with global atomics.
+// the planner chose (cheapest per rejected row first), then group keys and
+// metrics of the surviving rows aggregated per block (registers or shared
+// memory) and merged into int64 group slots with global atomics.
 //
 // This replaces, for one query, the reference's generated per-row loop
 // (codegen/template.cpp:61-89 filled by codegen/codegen.cpp:100-229), its
 // per-bulk host compaction (core/pipeline.cu:346-357) and its per-bulk
 // sort + reduce (core/pipeline.cu:360-472).
 //
-// Layout: a thread owns a group of 4 consecutive rows and reads each fact
-// column it needs with one 16-byte streaming load (ld.global.cs).  A column is
-// only fetched while some row of the group is still alive, so the columns
-// read after selective steps are mostly skipped.  Dimension tables small
-// enough are staged in shared memory at block start; the others are probed in
-// global memory through the read-only path and stay L2-resident.
+// Data movement: a persistent grid walks the fact rows in tiles of kTileRows.
+// In every block one producer warp streams each fact column the query reads
+// into a ring of shared-memory stages with 1-D bulk copies (cp.async.bulk,
+// completion counted on an mbarrier per stage); the consumer warps work on
+// the staged tile and release the stage.  The DRAM stream is therefore never
+// behind a dependent probe.  Small dimension tables are staged in shared
+// memory at block start; larger ones are probed in global memory and stay
+// L2-resident.
+//
+// Execution inside a tile is vectorised with selection vectors: each consumer
+// warp owns 128 rows.  The first step runs densely (4 rows per lane, one
+// 16-byte shared-memory read per column); the surviving rows are compacted
+// into a warp-local list (row offset + the payload words probed so far), and
+// every later step and the aggregation run over that list with all 32 lanes
+// busy.  Work per step is proportional to the rows still alive.
 #include <climits>
 
 #include "kern_common.cuh"
@@ -21,166 +30,345 @@
 
 namespace svm {
 
-constexpr int kStarThreads = 256;
+constexpr int kStarThreads = (kConsumerWarps + 1) * 32;
+constexpr uint32_t kWaitPolls = 1u << 22;
+constexpr int kListChunks = kWarpRows / 32;
 
-template <int kSlots>
-__device__ __forceinline__ int32_t pick(const int32_t (&val)[kMaxSteps][4], int slot, int j) {
-  int32_t raw = 0;
+struct StarSmem {
+  uint64_t full[kStages];
+  uint64_t empty[kStages];
+  long long red[kConsumerWarps][kMaxMetrics + 1];
+};
+
+// A consumer warp's selection vector: surviving row offsets (within the
+// warp's 128 rows), and per probed dimension the matched table entry of each
+// row, indexed by row offset (so compaction only moves the offsets).
+struct WarpList {
+  uint32_t pw[kMaxDims][kWarpRows];
+  uint16_t row[kWarpRows];
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Dense-table entry for `key`, or 0 (bit 0 clear) when absent.
+__device__ __forceinline__ uint32_t dense_entry(const DimDesc& D, const uint32_t* w, int32_t key, bool live) {
+  uint32_t idx = (uint32_t)key - (uint32_t)D.key_min;
+  live = live && idx < D.span;
+  uint32_t bit = idx * (uint32_t)D.entry_bits;  // span * entry_bits < 2^32 (planner)
+  uint32_t word = live ? w[bit >> 5] : 0u;
+  return D.entry_bits == 32 ? word : (word >> (bit & 31)) & ((1u << D.entry_bits) - 1u);
+}
+
+__device__ __forceinline__ uint32_t hash_entry(const DimDesc& D, const uint32_t* w, int32_t key, bool live) {
+  if (!live) return 0u;
+  const uint32_t cmask = D.span - 1u;
+  uint32_t slot = mix32((uint32_t)key) & cmask;
+  for (uint32_t n = 0; n <= cmask; n++) {
+    uint2 kv = reinterpret_cast<const uint2*>(w)[slot];
+    if (kv.y == 0u) return 0u;
+    if ((int32_t)kv.x == key) return kv.y;
+    slot = (slot + 1u) & cmask;
+  }
+  return 0u;
+}
+
+// Looks up 4 keys (lanes' `live` flags) in table D; entries with bit 0 clear
+// are misses.  Dense lookups are issued together (4 loads in flight).
+__device__ __forceinline__ void lookup4(const DimDesc& D, const uint32_t* tables, const int32_t (&key)[4],
+                                        const bool (&live)[4], uint32_t (&e)[4]) {
+  // Fully unrolled over the 4 keys: the arrays stay in registers.
+  const uint32_t* w = D.smem_word_off >= 0 ? tables + D.smem_word_off : D.words;
+  if (D.layout == LAYOUT_DENSE) {
 #pragma unroll
-  for (int k = 0; k < kSlots; k++)
-    if (k == slot) raw = val[k][j];
-  return raw;
+    for (int j = 0; j < 4; j++) e[j] = dense_entry(D, w, key[j], live[j]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; j++) e[j] = hash_entry(D, w, key[j], live[j]);
+  }
 }
 
-__device__ __forceinline__ int32_t opnd_value(const StarParams& P, const int32_t (&val)[kMaxSteps][4],
-                                              int j, Operand o) {
-  int32_t raw = pick<kMaxSteps>(val, o.slot, j);
-  if (o.field < 0) return raw;
-  return payload_value(P.dims[P.steps[o.slot].dim], o.field, (uint32_t)raw);
+__device__ __forceinline__ int32_t opnd_value(const StarParams& P, const int32_t* wstage, int row,
+                                              const uint32_t (&pw)[kMaxDims], Operand o) {
+  if (o.field < 0) return wstage[o.slot * kTileRows + row];
+  uint32_t e = pw[0];
+#pragma unroll
+  for (int d = 1; d < kMaxDims; d++)
+    if (o.slot == d) e = pw[d];
+  return payload_value(P.dims[o.slot], o.field, e);
 }
 
-__device__ __forceinline__ int32_t metric_value(const StarParams& P, const Metric& M,
-                                                const int32_t (&val)[kMaxSteps][4], int j) {
-  if (M.form == MF_PROG) {
+template <bool kProg>
+__device__ __forceinline__ int32_t metric_value(const StarParams& P, const Metric& M, const int32_t* wstage,
+                                                int row, const uint32_t (&pw)[kMaxDims]) {
+  if (kProg && M.form == MF_PROG) {
     int32_t ov[16];
-    for (int q = 0; q < P.nopnd; q++) ov[q] = opnd_value(P, val, j, P.opnds[q]);
+    for (int q = 0; q < P.nopnd; q++) ov[q] = opnd_value(P, wstage, row, pw, P.opnds[q]);
     return eval_prog(M.prog, ov, P.error);
   }
-  uint32_t a = (uint32_t)opnd_value(P, val, j, M.a);
+  uint32_t a = (uint32_t)opnd_value(P, wstage, row, pw, M.a);
   if (M.form == MF_OPND) return (int32_t)a;
-  uint32_t b = (uint32_t)opnd_value(P, val, j, M.b);
+  uint32_t b = (uint32_t)opnd_value(P, wstage, row, pw, M.b);
   if (M.form == MF_ADD) return (int32_t)(a + b);
   if (M.form == MF_SUB) return (int32_t)(a - b);
   return (int32_t)(a * b);
 }
 
-template <int kAgg>
-__global__ void __launch_bounds__(kStarThreads) star_kernel(const __grid_constant__ StarParams P) {
-  extern __shared__ __align__(16) uint32_t smem[];
+template <int kAgg, bool kProg>
+__device__ __forceinline__ void aggregate_row(const StarParams& P, const int32_t* wstage, int row,
+                                              const uint32_t (&pw)[kMaxDims], long long (&acc)[kMaxMetrics + 1],
+                                              unsigned long long* s_sum, unsigned int* s_cnt) {
+  if (kProg) {
+    for (int q = 0; q < P.npost; q++) {
+      int32_t ov[16];
+      for (int o = 0; o < P.nopnd; o++) ov[o] = opnd_value(P, wstage, row, pw, P.opnds[o]);
+      if (!eval_prog(P.post[q], ov, P.error)) return;
+    }
+  }
+  const int nm = P.nmetrics;
+  if (kAgg == AGG_SCALAR) {
+#pragma unroll
+    for (int m = 0; m < kMaxMetrics; m++)
+      if (m < nm) acc[m] += (long long)metric_value<kProg>(P, P.metrics[m], wstage, row, pw);
+    acc[kMaxMetrics] += 1;
+    return;
+  }
+  const unsigned long long G = P.ngroups;
+  unsigned long long gi = 0;
+  for (int q = 0; q < P.nkeys; q++) {
+    uint32_t off = (uint32_t)opnd_value(P, wstage, row, pw, P.keys[q]) - (uint32_t)P.kmin[q];
+    if (off >= P.krange[q]) {
+      raise_error(P.error, DERR_KEY_RANGE);
+      return;
+    }
+    gi += (unsigned long long)off * P.kstride[q];
+  }
+  for (int m = 0; m < nm; m++) {
+    unsigned long long v = (unsigned long long)(long long)metric_value<kProg>(P, P.metrics[m], wstage, row, pw);
+    if (kAgg == AGG_DENSE_SMEM)
+      atomicAdd(s_sum + m * G + gi, v);
+    else
+      atomicAdd(P.sums + m * G + gi, v);
+  }
+  if (kAgg == AGG_DENSE_SMEM)
+    atomicAdd(s_cnt + gi, 1u);
+  else
+    atomicAdd(P.counts + gi, 1ull);
+}
 
-  // Stage the small dimension tables.
+// One filter step over the first n entries of the warp's selection vector
+// (kChunks * 32 >= n): each lane takes one entry per chunk, all lookups of
+// the step are issued before any is used, survivors are compacted in place.
+// Returns the new list length.
+template <int kChunks>
+__device__ __forceinline__ int list_step(const StarParams& P, const Step& st, const int32_t* wstage,
+                                         const uint32_t* tables, WarpList& L, int n, int lane, uint32_t lt) {
+  const uint32_t span = (uint32_t)st.hi - (uint32_t)st.lo;
+  int32_t key[4];
+  bool live[4];
+  uint16_t row[4];
+  uint32_t e[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    const int idx = 32 * c + lane;
+    live[c] = c < kChunks && idx < n;
+    row[c] = live[c] ? L.row[idx] : (uint16_t)0;
+    key[c] = live[c] ? wstage[st.col * kTileRows + row[c]] : 0;
+    live[c] = live[c] && (uint32_t)key[c] - (uint32_t)st.lo <= span;
+  }
+  if (st.kind == STEP_PROBE) {
+    const DimDesc& D = P.dims[st.dim];
+    const uint32_t* w = D.smem_word_off >= 0 ? tables + D.smem_word_off : D.words;
+    if (D.layout == LAYOUT_DENSE) {
+#pragma unroll
+      for (int c = 0; c < kChunks; c++) e[c] = dense_entry(D, w, key[c], live[c]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < kChunks; c++) e[c] = hash_entry(D, w, key[c], live[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < kChunks; c++) {
+      live[c] = live[c] && (e[c] & 1u);
+      if (live[c]) L.pw[st.dim][row[c]] = e[c];
+    }
+  }
+  int pos[4];
+  int m = 0;
+#pragma unroll
+  for (int c = 0; c < kChunks; c++) {
+    const uint32_t b = __ballot_sync(0xffffffffu, live[c]);
+    pos[c] = m + __popc(b & lt);
+    m += __popc(b);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int c = 0; c < kChunks; c++)
+    if (live[c]) L.row[pos[c]] = row[c];
+  __syncwarp();
+  return m;
+}
+
+template <int kAgg, bool kProg>
+__global__ void __launch_bounds__(kStarThreads, 2) star_kernel(const __grid_constant__ StarParams P) {
+  extern __shared__ __align__(128) uint8_t dyn[];
+  __shared__ StarSmem S;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ncols = P.ncols, nst = P.nstages;
+  const size_t ring_bytes = (size_t)nst * ncols * kTileRows * 4;
+  int32_t* ring = reinterpret_cast<int32_t*>(dyn);
+  WarpList* lists = reinterpret_cast<WarpList*>(dyn + ring_bytes);
+  uint32_t* tables = reinterpret_cast<uint32_t*>(lists + kConsumerWarps);
+  unsigned long long* s_sum =
+      reinterpret_cast<unsigned long long*>(tables + ((P.smem_table_words + 3) & ~3));
+  const int nm = P.nmetrics;
+  const unsigned long long G = P.ngroups;
+  unsigned int* s_cnt = reinterpret_cast<unsigned int*>(s_sum + (kAgg == AGG_DENSE_SMEM ? nm * G : 0));
+
+  if (tid == 0) {
+    for (int s = 0; s < nst; s++) {
+      mbar_init(&S.full[s], 1);
+      mbar_init(&S.empty[s], kConsumerWarps);
+    }
+    mbar_fence_init();
+  }
   for (int d = 0; d < P.ndims; d++) {
     const DimDesc& D = P.dims[d];
     if (D.smem_word_off < 0) continue;
-    for (uint32_t w = threadIdx.x; w < D.table_words; w += blockDim.x)
-      smem[D.smem_word_off + w] = __ldg(D.words + w);
+    for (uint32_t w = tid; w < D.table_words; w += blockDim.x) tables[D.smem_word_off + w] = __ldg(D.words + w);
   }
-  const int nm = P.nmetrics;
-  const unsigned long long G = P.ngroups;
-  unsigned long long* s_sum = reinterpret_cast<unsigned long long*>(smem + ((P.smem_table_words + 3) & ~3));
-  unsigned int* s_cnt = reinterpret_cast<unsigned int*>(s_sum + (kAgg == AGG_DENSE_SMEM ? nm * G : 0));
   if (kAgg == AGG_DENSE_SMEM) {
-    for (unsigned long long i = threadIdx.x; i < nm * G; i += blockDim.x) s_sum[i] = 0ull;
-    for (unsigned long long i = threadIdx.x; i < G; i += blockDim.x) s_cnt[i] = 0u;
+    for (unsigned long long i = tid; i < nm * G; i += blockDim.x) s_sum[i] = 0ull;
+    for (unsigned long long i = tid; i < G; i += blockDim.x) s_cnt[i] = 0u;
   }
   __syncthreads();
 
-  long long acc[kMaxMetrics] = {0, 0, 0};
-  unsigned long long nacc = 0;
-
   const long long a0 = P.row_begin & ~3ll;
-  const long long ngr = (P.row_end - a0 + 3) >> 2;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ngr; g += stride) {
-    const long long r0 = a0 + 4 * g;
-    uint32_t mask = 0xFu;
-    if (r0 < P.row_begin) mask &= (0xFu << (P.row_begin - r0)) & 0xFu;
-    if (r0 + 4 > P.row_end) mask &= 0xFu >> (r0 + 4 - P.row_end);
-    int32_t val[kMaxSteps][4];
-#pragma unroll
-    for (int k = 0; k < kMaxSteps; k++) {
-      if (k < P.nsteps && mask) {
-        const Step& st = P.steps[k];
-        int4 v = __ldcs(reinterpret_cast<const int4*>(P.cols[st.col] + r0));
-        val[k][0] = v.x;
-        val[k][1] = v.y;
-        val[k][2] = v.z;
-        val[k][3] = v.w;
-        if (st.kind == STEP_RANGE) {
-          uint32_t span = (uint32_t)st.hi - (uint32_t)st.lo;
-#pragma unroll
-          for (int j = 0; j < 4; j++)
-            if ((uint32_t)val[k][j] - (uint32_t)st.lo > span) mask &= ~(1u << j);
-        } else if (st.kind == STEP_PROBE) {
-          const DimDesc& D = P.dims[st.dim];
-#pragma unroll
-          for (int j = 0; j < 4; j++) {
-            if (mask >> j & 1u) {
-              uint32_t e;
-              if (probe_dim(D, smem, val[k][j], e))
-                val[k][j] = (int32_t)e;
-              else
-                mask &= ~(1u << j);
-            }
-          }
+  const long long end4 = (P.row_end + 3) & ~3ll;  // copies stop at the 4-row boundary past row_end
+  const long long ntiles = (P.row_end - a0 + kTileRows - 1) / kTileRows;
+  long long acc[kMaxMetrics + 1] = {0, 0, 0, 0};
+
+  if (warp == kConsumerWarps) {
+    // ---------------- producer: one lane issues the bulk copies
+    if (lane == 0) {
+      long long issued = 0;
+      for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, issued++) {
+        int s = (int)(issued % nst);
+        long long k = issued / nst;
+        if (k > 0 && !mbar_wait_bounded(&S.empty[s], (uint32_t)((k - 1) & 1), kWaitPolls)) {
+          raise_error(P.error, DERR_TIMEOUT);
+          break;
         }
+        long long start = a0 + t * kTileRows;
+        long long stop = start + kTileRows < end4 ? start + kTileRows : end4;
+        uint32_t bytes = (uint32_t)((stop - start) * 4);
+        mbar_arrive_expect_tx(&S.full[s], bytes * (uint32_t)ncols);
+        for (int c = 0; c < ncols; c++)
+          bulk_g2s(ring + ((size_t)s * ncols + c) * kTileRows, P.cols[c] + start, bytes, &S.full[s]);
       }
+      // Every issued copy lands before the block exits.
+      long long first = issued > nst ? issued - nst : 0;
+      for (long long q = first; q < issued; q++)
+        mbar_wait_bounded(&S.full[q % nst], (uint32_t)((q / nst) & 1), kWaitPolls);
     }
-    if (!mask) continue;
+  } else {
+    // ---------------- consumers
+    WarpList& L = lists[warp];
+    const uint32_t lt = lanemask_lt();
+    long long i = 0;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
+      int s = (int)(i % nst);
+      if (!mbar_wait_bounded(&S.full[s], (uint32_t)((i / nst) & 1), kWaitPolls)) {
+        raise_error(P.error, DERR_TIMEOUT);
+        break;
+      }
+      // This warp's rows: [start + 128*warp, +128); lane owns 4 of them in the dense step.
+      const int32_t* wstage = ring + (size_t)s * ncols * kTileRows + warp * kWarpRows;
+      const long long r0 = a0 + t * kTileRows + warp * kWarpRows + 4 * lane;
+      uint32_t mask = 0xFu;
+      if (r0 < P.row_begin) mask &= (0xFu << (unsigned)(P.row_begin - r0 > 4 ? 4 : P.row_begin - r0)) & 0xFu;
+      if (r0 + 4 > P.row_end) mask &= r0 >= P.row_end ? 0u : 0xFu >> (unsigned)(r0 + 4 - P.row_end);
+
+      // ---- dense first step over the warp's 128 rows
+      uint32_t e0[4] = {0u, 0u, 0u, 0u};
+      int d0 = -1;
+      if (P.nsteps > 0) {
+        const Step& st = P.steps[0];
+        const int4 v = reinterpret_cast<const int4*>(wstage + st.col * kTileRows)[lane];
+        const int32_t key[4] = {v.x, v.y, v.z, v.w};
+        const uint32_t span = (uint32_t)st.hi - (uint32_t)st.lo;
+        bool live[4];
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      if (!(mask >> j & 1u)) continue;
-      bool keep = true;
-      for (int q = 0; q < P.npost && keep; q++) {
-        int32_t ov[16];
-        for (int o = 0; o < P.nopnd; o++) ov[o] = opnd_value(P, val, j, P.opnds[o]);
-        keep = eval_prog(P.post[q], ov, P.error) != 0;
+        for (int j = 0; j < 4; j++) {
+          live[j] = (mask >> j & 1u) && (uint32_t)key[j] - (uint32_t)st.lo <= span;
+        }
+        if (st.kind == STEP_PROBE) {
+          d0 = st.dim;
+          lookup4(P.dims[st.dim], tables, key, live, e0);
+#pragma unroll
+          for (int j = 0; j < 4; j++) live[j] = live[j] && (e0[j] & 1u);
+        }
+        mask = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) mask |= (uint32_t)live[j] << j;
       }
-      if (!keep) continue;
-      if (kAgg == AGG_SCALAR) {
-        for (int m = 0; m < nm; m++) acc[m] += (long long)metric_value(P, P.metrics[m], val, j);
-        nacc++;
-      } else {
-        unsigned long long gi = 0;
-        bool ok = true;
-        for (int q = 0; q < P.nkeys; q++) {
-          uint32_t off = (uint32_t)opnd_value(P, val, j, P.keys[q]) - (uint32_t)P.kmin[q];
-          ok &= off < P.krange[q];
-          gi += (unsigned long long)off * P.kstride[q];
-        }
-        if (!ok) {
-          raise_error(P.error, 3);
-          continue;
-        }
-        for (int m = 0; m < nm; m++) {
-          unsigned long long v = (unsigned long long)(long long)metric_value(P, P.metrics[m], val, j);
-          if (kAgg == AGG_DENSE_SMEM)
-            atomicAdd(s_sum + m * G + gi, v);
-          else
-            atomicAdd(P.sums + m * G + gi, v);
-        }
-        if (kAgg == AGG_DENSE_SMEM)
-          atomicAdd(s_cnt + gi, 1u);
+      if (d0 >= 0)
+        *reinterpret_cast<uint4*>(&L.pw[d0][4 * lane]) = make_uint4(e0[0], e0[1], e0[2], e0[3]);
+      int n = 0;
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const uint32_t b = __ballot_sync(0xffffffffu, mask >> j & 1u);
+        if (mask >> j & 1u) L.row[n + __popc(b & lt)] = (uint16_t)(4 * lane + j);
+        n += __popc(b);
+      }
+      __syncwarp();
+
+      // ---- later steps over the selection vector (all lanes busy)
+      for (int k = 1; k < P.nsteps && n > 0; k++) {
+        const Step& st = P.steps[k];
+        if (n <= 32)
+          n = list_step<1>(P, st, wstage, tables, L, n, lane, lt);
+        else if (n <= 64)
+          n = list_step<2>(P, st, wstage, tables, L, n, lane, lt);
         else
-          atomicAdd(P.counts + gi, 1ull);
+          n = list_step<4>(P, st, wstage, tables, L, n, lane, lt);
       }
+
+      // ---- aggregate the survivors, one per lane
+      for (int base = 0; base < n; base += 32) {
+        const int idx = base + lane;
+        if (idx < n) {
+          const int row = L.row[idx];
+          uint32_t pw[kMaxDims];
+#pragma unroll
+          for (int d = 0; d < kMaxDims; d++) pw[d] = d < P.ndims ? L.pw[d][row] : 0u;
+          aggregate_row<kAgg, kProg>(P, wstage, row, pw, acc, s_sum, s_cnt);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&S.empty[s]);
     }
   }
 
   if (kAgg == AGG_SCALAR) {
-    __shared__ long long red[kStarThreads / 32][kMaxMetrics + 1];
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    long long c = (long long)nacc;
-    for (int o = 16; o; o >>= 1) {
-      for (int m = 0; m < kMaxMetrics; m++) acc[m] += __shfl_xor_sync(0xffffffffu, acc[m], o);
-      c += __shfl_xor_sync(0xffffffffu, c, o);
-    }
-    if (lane == 0) {
-      for (int m = 0; m < kMaxMetrics; m++) red[wid][m] = acc[m];
-      red[wid][kMaxMetrics] = c;
-    }
+    for (int o = 16; o; o >>= 1)
+      for (int m = 0; m <= kMaxMetrics; m++) acc[m] += __shfl_xor_sync(0xffffffffu, acc[m], o);
+    if (lane == 0 && warp < kConsumerWarps)
+      for (int m = 0; m <= kMaxMetrics; m++) S.red[warp][m] = acc[m];
     __syncthreads();
-    if (threadIdx.x == 0) {
-      long long t[kMaxMetrics + 1] = {0, 0, 0, 0};
-      for (int w = 0; w < kStarThreads / 32; w++)
-        for (int m = 0; m <= kMaxMetrics; m++) t[m] += red[w][m];
+    if (tid == 0) {
+      long long tot[kMaxMetrics + 1] = {0, 0, 0, 0};
+      for (int w = 0; w < kConsumerWarps; w++)
+        for (int m = 0; m <= kMaxMetrics; m++) tot[m] += S.red[w][m];
       for (int m = 0; m < nm; m++)
-        if (t[m]) atomicAdd(P.sums + m, (unsigned long long)t[m]);
-      if (t[kMaxMetrics]) atomicAdd(P.counts, (unsigned long long)t[kMaxMetrics]);
+        if (tot[m]) atomicAdd(P.sums + m, (unsigned long long)tot[m]);
+      if (tot[kMaxMetrics]) atomicAdd(P.counts, (unsigned long long)tot[kMaxMetrics]);
     }
   } else if (kAgg == AGG_DENSE_SMEM) {
     __syncthreads();
-    for (unsigned long long i = threadIdx.x; i < G; i += blockDim.x) {
+    for (unsigned long long i = tid; i < G; i += blockDim.x) {
       unsigned int c = s_cnt[i];
       if (!c) continue;
       atomicAdd(P.counts + i, (unsigned long long)c);
@@ -192,48 +380,64 @@ __global__ void __launch_bounds__(kStarThreads) star_kernel(const __grid_constan
 int star_block_size() { return kStarThreads; }
 
 size_t star_smem_bytes(const StarParams& p) {
-  size_t b = (size_t)((p.smem_table_words + 3) & ~3) * 4;
+  size_t b = (size_t)p.nstages * p.ncols * kTileRows * 4;
+  b += sizeof(WarpList) * kConsumerWarps;
+  b += (size_t)((p.smem_table_words + 3) & ~3) * 4;
   if (p.agg == AGG_DENSE_SMEM) b += (size_t)p.ngroups * (8 * p.nmetrics + 4);
   return b;
 }
 
-template <int kAgg>
-static const void* star_fn() {
-  return reinterpret_cast<const void*>(&star_kernel<kAgg>);
+// Plans without bytecode (no residual predicate, no general metric) run the
+// lean instantiation.
+static bool plan_needs_prog(const StarParams& p) {
+  if (p.npost > 0) return true;
+  for (int m = 0; m < p.nmetrics; m++)
+    if (p.metrics[m].form == MF_PROG) return true;
+  return false;
 }
 
-static const void* star_entry(int agg) {
+template <bool kProg>
+static const void* star_entry_t(int agg) {
   switch (agg) {
-    case AGG_SCALAR: return star_fn<AGG_SCALAR>();
-    case AGG_DENSE_SMEM: return star_fn<AGG_DENSE_SMEM>();
-    default: return star_fn<AGG_DENSE_GLOBAL>();
+    case AGG_SCALAR: return reinterpret_cast<const void*>(&star_kernel<AGG_SCALAR, kProg>);
+    case AGG_DENSE_SMEM: return reinterpret_cast<const void*>(&star_kernel<AGG_DENSE_SMEM, kProg>);
+    default: return reinterpret_cast<const void*>(&star_kernel<AGG_DENSE_GLOBAL, kProg>);
   }
 }
 
-int star_grid_size(const StarParams& p, size_t smem) {
-  static bool attr_set[3] = {false, false, false};
-  int a = p.agg == AGG_SCALAR ? 0 : p.agg == AGG_DENSE_SMEM ? 1 : 2;
-  const void* fn = star_entry(p.agg);
+int star_blocks_per_sm(const StarParams& p, size_t smem) {
+  static bool attr_set[6] = {false, false, false, false, false, false};
+  const bool prog = plan_needs_prog(p);
+  int a = (p.agg == AGG_SCALAR ? 0 : p.agg == AGG_DENSE_SMEM ? 1 : 2) + (prog ? 3 : 0);
+  const void* fn = prog ? star_entry_t<true>(p.agg) : star_entry_t<false>(p.agg);
   if (!attr_set[a]) {
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024);
     attr_set[a] = true;
   }
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kStarThreads, smem);
+  return per_sm;
+}
+
+int star_grid_size(const StarParams& p, size_t smem) {
+  int per_sm = star_blocks_per_sm(p, smem);
   if (per_sm < 1) per_sm = 1;
-  long long groups = (p.row_end - (p.row_begin & ~3ll) + 3) >> 2;
-  long long want = (groups + kStarThreads - 1) / kStarThreads;
+  long long tiles = (p.row_end - (p.row_begin & ~3ll) + kTileRows - 1) / kTileRows;
   long long cap = (long long)num_sms() * per_sm;
-  if (want < 1) want = 1;
-  return (int)(want < cap ? want : cap);
+  if (tiles < 1) tiles = 1;
+  return (int)(tiles < cap ? tiles : cap);
 }
 
 cudaError_t launch_star(const StarParams& p, int grid, int block, size_t smem, cudaStream_t s) {
   note_launch();
-  switch (p.agg) {
-    case AGG_SCALAR: star_kernel<AGG_SCALAR><<<grid, block, smem, s>>>(p); break;
-    case AGG_DENSE_SMEM: star_kernel<AGG_DENSE_SMEM><<<grid, block, smem, s>>>(p); break;
-    case AGG_DENSE_GLOBAL: star_kernel<AGG_DENSE_GLOBAL><<<grid, block, smem, s>>>(p); break;
+  const bool prog = plan_needs_prog(p);
+  switch (p.agg * 2 + (prog ? 1 : 0)) {
+    case AGG_SCALAR * 2: star_kernel<AGG_SCALAR, false><<<grid, block, smem, s>>>(p); break;
+    case AGG_SCALAR * 2 + 1: star_kernel<AGG_SCALAR, true><<<grid, block, smem, s>>>(p); break;
+    case AGG_DENSE_SMEM * 2: star_kernel<AGG_DENSE_SMEM, false><<<grid, block, smem, s>>>(p); break;
+    case AGG_DENSE_SMEM * 2 + 1: star_kernel<AGG_DENSE_SMEM, true><<<grid, block, smem, s>>>(p); break;
+    case AGG_DENSE_GLOBAL * 2: star_kernel<AGG_DENSE_GLOBAL, false><<<grid, block, smem, s>>>(p); break;
+    case AGG_DENSE_GLOBAL * 2 + 1: star_kernel<AGG_DENSE_GLOBAL, true><<<grid, block, smem, s>>>(p); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

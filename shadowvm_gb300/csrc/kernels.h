@@ -69,6 +69,7 @@ cudaError_t launch_build_hash(const BuildInput& in, const DimDesc& d, unsigned l
 // ---- fused star query (kern_star.cu)
 cudaError_t launch_star(const StarParams& p, int grid, int block, size_t smem, cudaStream_t s);
 int star_block_size();
+int star_blocks_per_sm(const StarParams& p, size_t smem);
 int star_grid_size(const StarParams& p, size_t smem);
 size_t star_smem_bytes(const StarParams& p);
 // Compact non-empty groups in key order: writes keys (nkeys int32 columns),

@@ -365,7 +365,10 @@ svm_status build_dim(Ctx* x, const ObjectPtr& obj, int key_col, const std::vecto
   while (cap < 2 * T->live) cap <<= 1;
   unsigned long long dense_bytes = (span * entry_bits + 31) / 32 * 4;
   unsigned long long hash_bytes = cap * 8;
-  bool dense = span <= (1ull << 32) - 1 && dense_bytes <= std::max(2 * hash_bytes, 64ull << 10);
+  // Dense when it is not much larger than the hash table would be; the
+  // kernels index dense tables with 32-bit bit offsets.
+  bool dense = span * (unsigned long long)entry_bits < (1ull << 32) &&
+               dense_bytes <= std::max(2 * hash_bytes, 64ull << 10);
   d.key_min = T->key_min;
   x->scratch_reset();
   if (dense) {
@@ -533,117 +536,23 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
     if (st) return st;
   }
 
-  // ---- steps
+  // ---- staged fact columns: every fact column the query reads
   StarParams P{};
   P.error = x->d_error;
   P.row_begin = (long long)src->row0;
   P.row_end = (long long)(src->row0 + src->nrows);
-  std::vector<int> fact_cols;  // distinct fact columns -> StarParams::cols index
-  auto col_index = [&](int c) {
+  std::vector<int> fact_cols;  // StarParams::cols slot -> fact column
+  auto col_slot = [&](int c) {
     for (size_t i = 0; i < fact_cols.size(); i++)
       if (fact_cols[i] == c) return (int)i;
     fact_cols.push_back(c);
     return (int)fact_cols.size() - 1;
   };
-  std::vector<StepPlan> plan;
   std::vector<int> dim_of_obj(nref + 1, -1);
   int ndims = 0;
-  // Probe steps (with any range on the same fact column folded in).
-  std::set<int> ranged_done;
-  for (int k = 1; k <= nref; k++) {
-    if (join_of_obj[k] < 0) continue;
-    int lc = b.join_lkey[join_of_obj[k]].col;
-    StepPlan sp{};
-    sp.step.kind = STEP_PROBE;
-    sp.step.col = col_index(lc);
-    sp.step.lo = INT_MIN;
-    sp.step.hi = INT_MAX;
-    sp.step.dim = ndims;
-    dim_of_obj[k] = ndims++;
-    const DimTablePtr& T = tables[k];
-    unsigned long long base_rows = std::max<unsigned long long>(1, refs[k - 1]->source_rows);
-    sp.est = std::min(1.0, (double)T->live / (double)base_rows);
-    auto r = ranges.find(lc);
-    if (r != ranges.end() && !ranged_done.count(lc)) {
-      sp.step.lo = r->second.first;
-      sp.step.hi = r->second.second;
-      ranged_done.insert(lc);
-      ColStats cs;
-      if ((st = x->column_stats(src, lc, &cs))) return st;
-      double w = (double)cs.max - cs.min + 1;
-      double ov = std::max(0.0, (double)std::min(cs.max, r->second.second) - std::max(cs.min, r->second.first) + 1);
-      sp.est *= ov / w;
-    }
-    sp.order_class = 0;
-    plan.push_back(sp);
-  }
-  for (auto& kv : ranges) {
-    if (ranged_done.count(kv.first)) continue;
-    StepPlan sp{};
-    sp.step.kind = STEP_RANGE;
-    sp.step.col = col_index(kv.first);
-    sp.step.lo = kv.second.first;
-    sp.step.hi = kv.second.second;
-    ColStats cs;
-    if ((st = x->column_stats(src, kv.first, &cs))) return st;
-    double w = (double)cs.max - cs.min + 1;
-    double ov = std::max(0.0, (double)std::min(cs.max, kv.second.second) - std::max(cs.min, kv.second.first) + 1);
-    sp.est = ov / w;
-    sp.order_class = 0;
-    plan.push_back(sp);
-  }
-  std::stable_sort(plan.begin(), plan.end(), [](const StepPlan& a, const StepPlan& z) {
-    if (a.order_class != z.order_class) return a.order_class < z.order_class;
-    return a.est < z.est;
-  });
-  // Operands: fact columns read raw need a step whose slot keeps the raw
-  // value (a RANGE step does; a PROBE step replaces it with the entry).
-  std::vector<ColRef> all_refs = met_refs;
-  for (auto& r : b.reduce_key)
-    if (std::find(all_refs.begin(), all_refs.end(), r) == all_refs.end()) all_refs.push_back(r);
-  std::vector<ColRef> resid_refs;
-  for (int c : residual) collect_refs(pred, c, &resid_refs);
-  for (auto& r : resid_refs)
-    if (std::find(all_refs.begin(), all_refs.end(), r) == all_refs.end()) all_refs.push_back(r);
-  auto raw_slot = [&](int fact_col) -> int {
-    for (size_t s = 0; s < plan.size(); s++)
-      if (plan[s].step.kind != STEP_PROBE && fact_cols[plan[s].step.col] == fact_col) return (int)s;
-    return -1;
-  };
-  for (auto& r : all_refs) {
-    if (r.obj != 0 || raw_slot(r.col) >= 0) continue;
-    StepPlan sp{};
-    sp.step.kind = STEP_LOAD;
-    sp.step.col = col_index(r.col);
-    sp.step.lo = INT_MIN;
-    sp.step.hi = INT_MAX;
-    sp.est = 1.0;
-    sp.order_class = 1;
-    plan.push_back(sp);
-  }
-  if ((int)plan.size() > kMaxSteps || (int)fact_cols.size() > kMaxSteps)
-    return x->fail(SVM_E_UNSUPPORTED, "query touches more than 8 fact columns");
-  P.nsteps = (int)plan.size();
-  for (size_t s = 0; s < plan.size(); s++) P.steps[s] = plan[s].step;
-  for (size_t i = 0; i < fact_cols.size(); i++) P.cols[i] = (const int32_t*)src->base(fact_cols[i]);
-  auto operand_of = [&](const ColRef& r, Operand* o) -> bool {
-    if (r.obj == 0) {
-      int s = raw_slot(r.col);
-      if (s < 0) return false;
-      *o = Operand{(int8_t)s, -1};
-      return true;
-    }
-    int d = dim_of_obj[r.obj];
-    for (int s = 0; s < P.nsteps; s++)
-      if (P.steps[s].kind == STEP_PROBE && P.steps[s].dim == d) {
-        auto& pv = pay[r.obj];
-        int f = (int)(std::find(pv.begin(), pv.end(), r.col) - pv.begin());
-        *o = Operand{(int8_t)s, (int8_t)f};
-        return true;
-      }
-    return false;
-  };
-  // ---- dims into StarParams, small ones staged in shared memory
+  for (int k = 1; k <= nref; k++)
+    if (join_of_obj[k] >= 0) dim_of_obj[k] = ndims++;
+  // ---- dims into StarParams, the smallest staged in shared memory
   P.ndims = ndims;
   std::vector<std::pair<size_t, int>> by_size;
   for (int k = 1; k <= nref; k++) {
@@ -660,6 +569,78 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
     smem_words += (int)((bs.first / 4 + 3) & ~size_t(3));
   }
   P.smem_table_words = smem_words;
+  // ---- filter steps: probes (a range on the same column folded in) and ranges
+  struct StepPlan {
+    Step step;
+    double pass;   // expected fraction of rows that survive the step
+    double cost;   // relative cost per row tested
+  };
+  auto range_pass = [&](int col, int32_t lo, int32_t hi, double* pass) -> svm_status {
+    ColStats cs;
+    svm_status s = x->column_stats(src, col, &cs);
+    if (s) return s;
+    double w = (double)cs.max - cs.min + 1;
+    double ov = std::max(0.0, (double)std::min(cs.max, hi) - std::max(cs.min, lo) + 1);
+    *pass = ov / w;
+    return SVM_OK;
+  };
+  std::vector<StepPlan> plan;
+  std::set<int> ranged_done;
+  for (int k = 1; k <= nref; k++) {
+    if (join_of_obj[k] < 0) continue;
+    int lc = b.join_lkey[join_of_obj[k]].col;
+    StepPlan sp{};
+    sp.step.kind = STEP_PROBE;
+    sp.step.col = col_slot(lc);
+    sp.step.lo = INT_MIN;
+    sp.step.hi = INT_MAX;
+    sp.step.dim = dim_of_obj[k];
+    const DimTablePtr& T = tables[k];
+    unsigned long long base_rows = std::max<unsigned long long>(1, refs[k - 1]->source_rows);
+    sp.pass = std::min(1.0, (double)T->live / (double)base_rows);
+    sp.cost = P.dims[sp.step.dim].smem_word_off >= 0 ? 1.0 : 4.0;
+    auto r = ranges.find(lc);
+    if (r != ranges.end()) {
+      sp.step.lo = r->second.first;
+      sp.step.hi = r->second.second;
+      ranged_done.insert(lc);
+      double rp;
+      if ((st = range_pass(lc, r->second.first, r->second.second, &rp))) return st;
+      sp.pass *= rp;
+    }
+    plan.push_back(sp);
+  }
+  for (auto& kv : ranges) {
+    if (ranged_done.count(kv.first)) continue;
+    StepPlan sp{};
+    sp.step.kind = STEP_RANGE;
+    sp.step.col = col_slot(kv.first);
+    sp.step.lo = kv.second.first;
+    sp.step.hi = kv.second.second;
+    sp.cost = 0.25;
+    if ((st = range_pass(kv.first, kv.second.first, kv.second.second, &sp.pass))) return st;
+    plan.push_back(sp);
+  }
+  // Independent filters: ascending cost / (1 - pass) minimises the expected
+  // work per row.
+  std::stable_sort(plan.begin(), plan.end(), [](const StepPlan& a, const StepPlan& z) {
+    return a.cost / std::max(1e-6, 1.0 - a.pass) < z.cost / std::max(1e-6, 1.0 - z.pass);
+  });
+  if ((int)plan.size() > kMaxSteps) return x->fail(SVM_E_UNSUPPORTED, "more than 8 filter steps");
+  P.nsteps = (int)plan.size();
+  for (size_t s = 0; s < plan.size(); s++) P.steps[s] = plan[s].step;
+  auto operand_of = [&](const ColRef& r, Operand* o) -> bool {
+    if (r.obj == 0) {
+      *o = Operand{(int8_t)col_slot(r.col), -1};
+      return true;
+    }
+    int d = dim_of_obj[r.obj];
+    if (d < 0) return false;
+    auto& pv = pay[r.obj];
+    int f = (int)(std::find(pv.begin(), pv.end(), r.col) - pv.begin());
+    *o = Operand{(int8_t)d, (int8_t)f};
+    return true;
+  };
   // ---- operand table for bytecode programs
   std::vector<ColRef> prog_refs;
   auto add_prog_refs = [&](const Expr& e, int node) { collect_refs(e, node, &prog_refs); };
@@ -728,6 +709,10 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   else
     P.agg = AGG_DENSE_GLOBAL;
 
+  if ((int)fact_cols.size() > kMaxSteps) return x->fail(SVM_E_UNSUPPORTED, "query reads more than 8 fact columns");
+  P.ncols = (int)fact_cols.size();
+  for (size_t i = 0; i < fact_cols.size(); i++) P.cols[i] = (const int32_t*)src->base(fact_cols[i]);
+
   // ---- scratch: sums + counts (+ finalize buffers)
   x->scratch_reset();
   size_t agg_bytes = 8 * (size_t)G * (nmet + 1);
@@ -744,8 +729,20 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   if (e) return x->cuda_fail(e, "cudaMemsetAsync");
   if (empty) P.row_end = P.row_begin;  // a contradictory filter: no row can pass
 
+  // Ring depth: the most resident blocks per SM, then the deepest ring.
+  int best_blocks = 0, best_st = 0;
+  for (int nst = kStages; nst >= 2; nst--) {
+    P.nstages = nst;
+    size_t sm = star_smem_bytes(P);
+    int blocks = sm <= 200 * 1024 ? star_blocks_per_sm(P, sm) : 0;
+    if (blocks > best_blocks) {
+      best_blocks = blocks;
+      best_st = nst;
+    }
+  }
+  if (best_blocks == 0) return x->fail(SVM_E_UNSUPPORTED, "shared-memory plan too large");
+  P.nstages = best_st;
   size_t smem = star_smem_bytes(P);
-  if (smem > 200 * 1024) return x->fail(SVM_E_UNSUPPORTED, "shared-memory plan too large");
   int grid = star_grid_size(P, smem);
   cudaEvent_t ev;
   x->prof_begin(SVM_K_STAR, &ev);

@@ -41,11 +41,11 @@ struct Prog {
   int32_t konst[16];
 };
 
-// Operand reference: either a fact column value held in step slot `slot`, or
-// a payload field of the dimension probed in step slot `slot`.
+// Operand reference: a fact column (staged column slot) or a payload field of
+// a probed dimension.
 struct Operand {
-  int8_t slot;     // step index holding the fact value / payload word
-  int8_t field;    // -1: the fact value itself; >= 0: payload field index
+  int8_t slot;     // field < 0: staged fact column slot; else dimension index
+  int8_t field;    // -1: fact value; >= 0: payload field of dimension `slot`
 };
 
 // ---------------------------------------------------------------- dimension tables
@@ -81,14 +81,21 @@ __host__ __device__ inline uint32_t mix32(uint32_t x) {
 }
 
 // ---------------------------------------------------------------- fused star query
-enum StepKind : int { STEP_RANGE = 0, STEP_PROBE = 1, STEP_LOAD = 2 };
+enum StepKind : int { STEP_RANGE = 0, STEP_PROBE = 1 };
 
 struct Step {
   int kind;
-  int col;          // fact column index into StarParams::cols
-  int32_t lo, hi;   // STEP_RANGE: keep lo <= v <= hi
-  int dim;          // STEP_PROBE
+  int col;          // staged fact column slot (index into StarParams::cols)
+  int32_t lo, hi;   // keep lo <= v <= hi (PROBE steps too; full range = no check)
+  int dim;          // STEP_PROBE: dimension index
 };
+
+// The scan streams every fact column the query reads through a ring of
+// shared-memory stages: tiles of kTileRows rows, one bulk copy per column.
+constexpr int kConsumerWarps = 8;
+constexpr int kWarpRows = 32 * 4;                     // 4 rows per consumer lane
+constexpr int kTileRows = kConsumerWarps * kWarpRows;
+constexpr int kStages = 4;                            // at most; StarParams::nstages in use
 
 enum MetricForm : int { MF_OPND = 0, MF_ADD = 1, MF_SUB = 2, MF_MUL = 3, MF_PROG = 4 };
 
@@ -102,6 +109,8 @@ enum AggMode : int { AGG_SCALAR = 0, AGG_DENSE_SMEM = 1, AGG_DENSE_GLOBAL = 2, A
 
 struct StarParams {
   const int32_t* cols[kMaxSteps];   // fact column base pointers (row 0 of the base allocation)
+  int ncols;                        // staged columns
+  int nstages;                      // ring depth (2..kStages)
   long long row_begin, row_end;     // rows [row_begin, row_end) of the base columns
   int nsteps;
   Step steps[kMaxSteps];
