@@ -32,7 +32,6 @@ namespace svm {
 
 constexpr int kStarThreads = (kConsumerWarps + 1) * 32;
 constexpr uint32_t kWaitPolls = 1u << 22;
-constexpr int kListChunks = kWarpRows / 32;
 
 struct StarSmem {
   uint64_t full[kStages];
