@@ -162,6 +162,61 @@ svm_status svm_run_pipeline(svm_ctx* ctx, const svm_pipeline* pipe);
  * equals its result from svm_run_pipeline. */
 svm_status svm_run_batch(svm_ctx* ctx, int n, const svm_pipeline* pipes);
 
+/* ---- allocation-free scan ---------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory on their query path: a host runtime that owns all device memory
+ * through its own pool, a thread that must not take the implicit device-wide
+ * synchronisation of cudaMalloc/cudaFree, or code that issues work while other
+ * streams must not be disturbed.  Every other entry point here allocates
+ * (object storage, dimension tables, the context's scratch arena); this one
+ * does not.
+ *
+ * It runs the same fused scan kernel as svm_run_pipeline, restricted to range
+ * filters on the given columns, dense group keys on those columns and
+ * SVM_METRIC_* metrics, over caller-owned device columns, and writes the
+ * non-empty groups sorted by key -- the rows svm_run_pipeline stores for the
+ * equivalent Filter/ReduceBy pipeline with Int64 metrics -- into
+ * caller-owned device buffers.  Its scratch (group slots, compaction flags
+ * and positions, the error word) is one static device array of
+ * SVM_NOALLOC_SCRATCH_WORDS 64-bit words (1 MiB) that every GPU which loads
+ * the library holds until the process exits; a query whose groups need more
+ * is rejected with SVM_E_INVALID_ARG.  The array is shared by all calls and
+ * keeps the last call's contents; each call clears what must start at zero.
+ * Calls whose work overlaps on the GPU (two host threads, or two contexts on
+ * one device) race on it: serialise them.  The first call on a device looks
+ * the array up (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  The call is synchronous on the
+ * context's stream.
+ *
+ * Inputs: cols[c] int32 device pointers, 16-byte aligned, readable up to
+ * nrows rounded up to a multiple of 4.  Outputs: key_out[k] (int32) and
+ * sum_out[m] (int64) device arrays of max_rows entries; *nrows_out (host) is
+ * the number of rows written (1 when there are no keys and nrows > 0). */
+#define SVM_NOALLOC_SCRATCH_WORDS (1u << 17)
+enum { SVM_METRIC_COL = 0, SVM_METRIC_ADD = 1, SVM_METRIC_SUB = 2, SVM_METRIC_MUL = 3 };
+
+typedef struct svm_noalloc_scan {
+  int ncols;
+  const int32_t* const* cols;
+  unsigned long long nrows;
+  int nranges;                 /* keep rows with range_lo[i] <= cols[range_col[i]] <= range_hi[i] */
+  const int* range_col;
+  const int* range_lo;
+  const int* range_hi;
+  int nkeys;                   /* 0..3 group keys; every value lies in [key_min, key_max] */
+  const int* key_col;
+  const int* key_min;
+  const int* key_max;
+  int nmetrics;                /* 1..3: metric_op applied to cols[metric_a] (and cols[metric_b]) */
+  const int* metric_op;
+  const int* metric_a;
+  const int* metric_b;
+} svm_noalloc_scan;
+
+svm_status svm_scan_aggregate_noalloc(svm_ctx* ctx, const svm_noalloc_scan* q, int32_t* const* key_out,
+                                      long long* const* sum_out, unsigned long long max_rows,
+                                      unsigned long long* nrows_out);
+
 /* ---- profiling -------------------------------------------------------------- */
 /* With profiling on, the library brackets each of its kernel launches with
  * CUDA events on its stream.  svm_profile_read reports, for kernel class k

@@ -45,6 +45,21 @@ class svm_pipeline(ctypes.Structure):
                 ("npre", ctypes.c_int), ("pre_pipeline_id", ctypes.POINTER(ctypes.c_char_p))]
 
 
+class svm_noalloc_scan(ctypes.Structure):
+    _fields_ = [("ncols", ctypes.c_int), ("cols", ctypes.POINTER(ctypes.c_void_p)),
+                ("nrows", ctypes.c_ulonglong),
+                ("nranges", ctypes.c_int), ("range_col", ctypes.POINTER(ctypes.c_int)),
+                ("range_lo", ctypes.POINTER(ctypes.c_int)), ("range_hi", ctypes.POINTER(ctypes.c_int)),
+                ("nkeys", ctypes.c_int), ("key_col", ctypes.POINTER(ctypes.c_int)),
+                ("key_min", ctypes.POINTER(ctypes.c_int)), ("key_max", ctypes.POINTER(ctypes.c_int)),
+                ("nmetrics", ctypes.c_int), ("metric_op", ctypes.POINTER(ctypes.c_int)),
+                ("metric_a", ctypes.POINTER(ctypes.c_int)), ("metric_b", ctypes.POINTER(ctypes.c_int))]
+
+
+METRIC_COL, METRIC_ADD, METRIC_SUB, METRIC_MUL = range(4)
+NOALLOC_SCRATCH_WORDS = 1 << 17
+
+
 class SvmError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"{STATUS.get(status, status)}: {message}")
@@ -94,6 +109,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "svm_profile_reset": (I, [P]),
         "svm_profile_read": (I, [P, I, ctypes.POINTER(U64), ctypes.POINTER(D)]),
         "svm_kernel_launches": (U64, []),
+        "svm_scan_aggregate_noalloc": (I, [P, ctypes.POINTER(svm_noalloc_scan), ctypes.POINTER(P),
+                                           ctypes.POINTER(P), U64, ctypes.POINTER(U64)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
