@@ -11,7 +11,8 @@ import os
 import re
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libshadowvm_gb300.so")
+# SVM_LIB overrides the library path (an alternate build of the same ABI).
+LIB_PATH = os.environ.get("SVM_LIB") or os.path.join(HERE, "_build", "libshadowvm_gb300.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "svm_capi.h")
 
 STATUS = {0: "SVM_OK", 1: "SVM_E_INVALID_ARG", 2: "SVM_E_UNSUPPORTED", 3: "SVM_E_OOM_BUDGET",

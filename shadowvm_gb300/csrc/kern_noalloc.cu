@@ -145,6 +145,7 @@ extern "C" svm_status svm_scan_aggregate_noalloc(svm_ctx* c, const svm_noalloc_s
   unsigned long long* scant = fin + fin_words;
   P.agg = nkeys == 0 ? AGG_SCALAR
                      : G * (8ull * nm + 4) <= (unsigned long long)kSmemAggBytes ? AGG_DENSE_SMEM : AGG_DENSE_GLOBAL;
+  flatten_plan(P);
   int best_blocks = 0, best_st = 0;
   for (int nst = kStages; nst >= 2; nst--) {
     P.nstages = nst;

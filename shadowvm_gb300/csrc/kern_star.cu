@@ -54,7 +54,7 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 }
 
 // Dense-table entry for `key`, or 0 (bit 0 clear) when absent.
-__device__ __forceinline__ uint32_t dense_entry(const DimDesc& D, const uint32_t* w, int32_t key, bool live) {
+__device__ __forceinline__ uint32_t dense_entry(const Step& D, const uint32_t* w, int32_t key, bool live) {
   uint32_t idx = (uint32_t)key - (uint32_t)D.key_min;
   live = live && idx < D.span;
   uint32_t bit = idx * (uint32_t)D.entry_bits;  // span * entry_bits < 2^32 (planner)
@@ -62,7 +62,7 @@ __device__ __forceinline__ uint32_t dense_entry(const DimDesc& D, const uint32_t
   return D.entry_bits == 32 ? word : (word >> (bit & 31)) & ((1u << D.entry_bits) - 1u);
 }
 
-__device__ __forceinline__ uint32_t hash_entry(const DimDesc& D, const uint32_t* w, int32_t key, bool live) {
+__device__ __forceinline__ uint32_t hash_entry(const Step& D, const uint32_t* w, int32_t key, bool live) {
   if (!live) return 0u;
   const uint32_t cmask = D.span - 1u;
   uint32_t slot = mix32((uint32_t)key) & cmask;
@@ -77,7 +77,7 @@ __device__ __forceinline__ uint32_t hash_entry(const DimDesc& D, const uint32_t*
 
 // Looks up 4 keys (lanes' `live` flags) in table D; entries with bit 0 clear
 // are misses.  Dense lookups are issued together (4 loads in flight).
-__device__ __forceinline__ void lookup4(const DimDesc& D, const uint32_t* tables, const int32_t (&key)[4],
+__device__ __forceinline__ void lookup4(const Step& D, const uint32_t* tables, const int32_t (&key)[4],
                                         const bool (&live)[4], uint32_t (&e)[4]) {
   // Fully unrolled over the 4 keys: the arrays stay in registers.
   const uint32_t* w = D.smem_word_off >= 0 ? tables + D.smem_word_off : D.words;
@@ -100,6 +100,19 @@ __device__ __forceinline__ int32_t opnd_value(const StarParams& P, const int32_t
   return payload_value(P.dims[o.slot], o.field, e);
 }
 
+// A flattened operand: one staged value or one payload field, no indirection.
+__device__ __forceinline__ uint32_t extract(const Extract& x, const int32_t* wstage, int row,
+                                            const uint32_t (&pw)[kMaxDims]) {
+  if (x.dim < 0) return (uint32_t)wstage[x.slot * kTileRows + row] + (uint32_t)x.base;
+  uint32_t e = pw[0];
+#pragma unroll
+  for (int d = 1; d < kMaxDims; d++)
+    if (x.dim == d) e = pw[d];
+  uint32_t v = (e >> x.shift) & x.mask;
+  if (x.col) v = (uint32_t)__ldg(x.col + v);
+  return v + (uint32_t)x.base;
+}
+
 template <bool kProg>
 __device__ __forceinline__ int32_t metric_value(const StarParams& P, const Metric& M, const int32_t* wstage,
                                                 int row, const uint32_t (&pw)[kMaxDims]) {
@@ -108,9 +121,9 @@ __device__ __forceinline__ int32_t metric_value(const StarParams& P, const Metri
     for (int q = 0; q < P.nopnd; q++) ov[q] = opnd_value(P, wstage, row, pw, P.opnds[q]);
     return eval_prog(M.prog, ov, P.error);
   }
-  uint32_t a = (uint32_t)opnd_value(P, wstage, row, pw, M.a);
+  uint32_t a = extract(M.xa, wstage, row, pw);
   if (M.form == MF_OPND) return (int32_t)a;
-  uint32_t b = (uint32_t)opnd_value(P, wstage, row, pw, M.b);
+  uint32_t b = extract(M.xb, wstage, row, pw);
   if (M.form == MF_ADD) return (int32_t)(a + b);
   if (M.form == MF_SUB) return (int32_t)(a - b);
   return (int32_t)(a * b);
@@ -136,62 +149,93 @@ __device__ __forceinline__ void aggregate_row(const StarParams& P, const int32_t
     return;
   }
   const unsigned long long G = P.ngroups;
-  unsigned long long gi = 0;
-  for (int q = 0; q < P.nkeys; q++) {
-    uint32_t off = (uint32_t)opnd_value(P, wstage, row, pw, P.keys[q]) - (uint32_t)P.kmin[q];
-    if (off >= P.krange[q]) {
-      raise_error(P.error, DERR_KEY_RANGE);
-      return;
+  // Dense group index (G <= 2^26): keys read through their flattened
+  // extractors with compile-time indices.
+  uint32_t gi = 0;
+  bool in_range = true;
+#pragma unroll
+  for (int q = 0; q < kMaxKeys; q++) {
+    if (q < P.nkeys) {
+      const uint32_t off = extract(P.kx[q], wstage, row, pw);
+      in_range &= off < P.krange[q];
+      gi += off * (uint32_t)P.kstride[q];
     }
-    gi += (unsigned long long)off * P.kstride[q];
   }
-  for (int m = 0; m < nm; m++) {
-    unsigned long long v = (unsigned long long)(long long)metric_value<kProg>(P, P.metrics[m], wstage, row, pw);
-    if (kAgg == AGG_DENSE_SMEM)
-      atomicAdd(s_sum + m * G + gi, v);
-    else
-      atomicAdd(P.sums + m * G + gi, v);
+  if (!in_range) {
+    raise_error(P.error, DERR_KEY_RANGE);
+    return;
   }
+#pragma unroll
+  for (int m = 0; m < kMaxMetrics; m++) {
+    if (m < nm) {
+      unsigned long long v = (unsigned long long)(long long)metric_value<kProg>(P, P.metrics[m], wstage, row, pw);
+      if (kAgg == AGG_DENSE_SMEM)
+        atomicAdd(s_sum + m * G + gi, v);
+      else
+        atomicAdd(P.sums + m * G + gi, v);
+    }
+  }
+  // Only "the group has a row" is read back: a plain store marks it.
   if (kAgg == AGG_DENSE_SMEM)
-    atomicAdd(s_cnt + gi, 1u);
+    s_cnt[gi] = 1u;
   else
     atomicAdd(P.counts + gi, 1ull);
 }
 
-// One filter step over the first n entries of the warp's selection vector
-// (kChunks * 32 >= n): each lane takes one entry per chunk, all lookups of
-// the step are issued before any is used, survivors are compacted in place.
-// Returns the new list length.
-template <int kChunks>
-__device__ __forceinline__ int list_step(const StarParams& P, const Step& st, const int32_t* wstage,
-                                         const uint32_t* tables, WarpList& L, int n, int lane, uint32_t lt) {
-  const uint32_t span = (uint32_t)st.hi - (uint32_t)st.lo;
-  int32_t key[4];
+// kFuse consecutive filter steps over the first n entries of the warp's
+// selection vector (kChunks * 32 >= n): each lane takes one entry per chunk;
+// every lookup of the fused steps is issued before any result is used (the
+// steps are evaluated independently and their outcomes AND-ed); survivors are
+// compacted in place.  Returns the new list length.
+template <int kChunks, int kFuse>
+__device__ __forceinline__ int list_step(const Step* sts, const int32_t* wstage, const uint32_t* tables,
+                                         WarpList& L, int n, int lane, uint32_t lt) {
   bool live[4];
   uint16_t row[4];
-  uint32_t e[4] = {0u, 0u, 0u, 0u};
+  uint32_t e[kFuse][4];
+  bool ok[kFuse][4];
 #pragma unroll
   for (int c = 0; c < 4; c++) {
     const int idx = 32 * c + lane;
     live[c] = c < kChunks && idx < n;
     row[c] = live[c] ? L.row[idx] : (uint16_t)0;
-    key[c] = live[c] ? wstage[st.col * kTileRows + row[c]] : 0;
-    live[c] = live[c] && (uint32_t)key[c] - (uint32_t)st.lo <= span;
   }
-  if (st.kind == STEP_PROBE) {
-    const DimDesc& D = P.dims[st.dim];
-    const uint32_t* w = D.smem_word_off >= 0 ? tables + D.smem_word_off : D.words;
-    if (D.layout == LAYOUT_DENSE) {
 #pragma unroll
-      for (int c = 0; c < kChunks; c++) e[c] = dense_entry(D, w, key[c], live[c]);
-    } else {
+  for (int f = 0; f < kFuse; f++) {
+    const Step& st = sts[f];
+    const uint32_t span = (uint32_t)st.hi - (uint32_t)st.lo;
+    int32_t key[4];
 #pragma unroll
-      for (int c = 0; c < kChunks; c++) e[c] = hash_entry(D, w, key[c], live[c]);
+    for (int c = 0; c < 4; c++) {
+      key[c] = live[c] ? wstage[st.col * kTileRows + row[c]] : 0;
+      ok[f][c] = live[c] && (uint32_t)key[c] - (uint32_t)st.lo <= span;
+      e[f][c] = 0u;
     }
+    if (st.kind == STEP_PROBE) {
+      const uint32_t* w = st.smem_word_off >= 0 ? tables + st.smem_word_off : st.words;
+      if (st.layout == LAYOUT_DENSE) {
 #pragma unroll
-    for (int c = 0; c < kChunks; c++) {
-      live[c] = live[c] && (e[c] & 1u);
-      if (live[c]) L.pw[st.dim][row[c]] = e[c];
+        for (int c = 0; c < kChunks; c++) e[f][c] = dense_entry(st, w, key[c], ok[f][c]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < kChunks; c++) e[f][c] = hash_entry(st, w, key[c], ok[f][c]);
+      }
+    }
+  }
+#pragma unroll
+  for (int f = 0; f < kFuse; f++) {
+    const Step& st = sts[f];
+#pragma unroll
+    for (int c = 0; c < kChunks; c++)
+      live[c] = live[c] && ok[f][c] && (st.kind != STEP_PROBE || (e[f][c] & 1u));
+  }
+#pragma unroll
+  for (int f = 0; f < kFuse; f++) {
+    const Step& st = sts[f];
+    if (st.kind == STEP_PROBE) {
+#pragma unroll
+      for (int c = 0; c < kChunks; c++)
+        if (live[c]) L.pw[st.dim][row[c]] = e[f][c];
     }
   }
   int pos[4];
@@ -305,7 +349,7 @@ __global__ void __launch_bounds__(kStarThreads, 2) star_kernel(const __grid_cons
         }
         if (st.kind == STEP_PROBE) {
           d0 = st.dim;
-          lookup4(P.dims[st.dim], tables, key, live, e0);
+          lookup4(st, tables, key, live, e0);
 #pragma unroll
           for (int j = 0; j < 4; j++) live[j] = live[j] && (e0[j] & 1u);
         }
@@ -326,13 +370,13 @@ __global__ void __launch_bounds__(kStarThreads, 2) star_kernel(const __grid_cons
 
       // ---- later steps over the selection vector (all lanes busy)
       for (int k = 1; k < P.nsteps && n > 0; k++) {
-        const Step& st = P.steps[k];
+        const Step* st = &P.steps[k];
         if (n <= 32)
-          n = list_step<1>(P, st, wstage, tables, L, n, lane, lt);
+          n = list_step<1, 1>(st, wstage, tables, L, n, lane, lt);
         else if (n <= 64)
-          n = list_step<2>(P, st, wstage, tables, L, n, lane, lt);
+          n = list_step<2, 1>(st, wstage, tables, L, n, lane, lt);
         else
-          n = list_step<4>(P, st, wstage, tables, L, n, lane, lt);
+          n = list_step<4, 1>(st, wstage, tables, L, n, lane, lt);
       }
 
       // ---- aggregate the survivors, one per lane

@@ -729,6 +729,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   if (e) return x->cuda_fail(e, "cudaMemsetAsync");
   if (empty) P.row_end = P.row_begin;  // a contradictory filter: no row can pass
 
+  flatten_plan(P);
   // Ring depth: the most resident blocks per SM, then the deepest ring.
   int best_blocks = 0, best_st = 0;
   for (int nst = kStages; nst >= 2; nst--) {
