@@ -486,6 +486,270 @@ cudaError_t launch_star(const StarParams& p, int grid, int block, size_t smem, c
   return cudaGetLastError();
 }
 
+// ================================================================ batched queries
+// One persistent launch for a batch of fact pipelines over one fact table.
+// The producer hands tiles out dynamically (an atomic tile counter, so blocks
+// that drew tiles covered by many queries take fewer tiles) and streams the
+// union of the batch's columns; a tile index of -1 in a stage ends the scan.
+// Each consumer warp then runs, for every query whose range covers its 128
+// rows, the same dense-step / selection-vector / aggregation pipeline as the
+// single-query kernel, into that query's own int64 slots.
+
+__device__ __forceinline__ void batch_query_slice(const BatchQuery& Q, const BatchParams& B, const int32_t* wstage,
+                                                  long long slice_start, WarpList& L, int lane, uint32_t lt) {
+  const long long r0 = slice_start + 4 * lane;
+  uint32_t mask = 0;
+#pragma unroll
+  for (int j = 0; j < 4; j++) mask |= (uint32_t)(r0 + j >= Q.row_begin && r0 + j < Q.row_end) << j;
+  if (!__any_sync(0xffffffffu, mask)) return;
+  uint32_t e0[4] = {0u, 0u, 0u, 0u};
+  int d0 = -1;
+  if (Q.nsteps > 0) {
+    const Step& st = Q.steps[0];
+    const int4 v = reinterpret_cast<const int4*>(wstage + st.col * kTileRows)[lane];
+    const int32_t key[4] = {v.x, v.y, v.z, v.w};
+    const uint32_t span = (uint32_t)st.hi - (uint32_t)st.lo;
+    bool live[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) live[j] = (mask >> j & 1u) && (uint32_t)key[j] - (uint32_t)st.lo <= span;
+    if (st.kind == STEP_PROBE) {
+      d0 = st.dim;
+      lookup4(st, nullptr, key, live, e0);
+#pragma unroll
+      for (int j = 0; j < 4; j++) live[j] = live[j] && (e0[j] & 1u);
+    }
+    mask = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) mask |= (uint32_t)live[j] << j;
+  }
+  __syncwarp();
+  if (d0 >= 0) *reinterpret_cast<uint4*>(&L.pw[d0][4 * lane]) = make_uint4(e0[0], e0[1], e0[2], e0[3]);
+  int n = 0;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const uint32_t b = __ballot_sync(0xffffffffu, mask >> j & 1u);
+    if (mask >> j & 1u) L.row[n + __popc(b & lt)] = (uint16_t)(4 * lane + j);
+    n += __popc(b);
+  }
+  __syncwarp();
+  for (int k = 1; k < Q.nsteps && n > 0; k++) {
+    const Step* st = &Q.steps[k];
+    if (n <= 32)
+      n = list_step<1, 1>(st, wstage, nullptr, L, n, lane, lt);
+    else if (n <= 64)
+      n = list_step<2, 1>(st, wstage, nullptr, L, n, lane, lt);
+    else
+      n = list_step<4, 1>(st, wstage, nullptr, L, n, lane, lt);
+  }
+  if (n == 0) return;
+  unsigned long long* sums = B.slots + Q.slot_off;
+  const unsigned long long G = Q.ngroups;
+  const int nm = Q.nmetrics;
+  long long acc[kMaxMetrics] = {0, 0, 0};
+  for (int base = 0; base < n; base += 32) {
+    const int idx = base + lane;
+    if (idx >= n) continue;
+    const int row = L.row[idx];
+    uint32_t pw[kMaxDims];
+#pragma unroll
+    for (int d = 0; d < kMaxDims; d++) pw[d] = L.pw[d][row];
+    uint32_t gi = 0;
+    bool in_range = true;
+#pragma unroll
+    for (int q = 0; q < kMaxKeys; q++) {
+      if (q < Q.nkeys) {
+        const uint32_t off = extract(Q.kx[q], wstage, row, pw);
+        in_range &= off < Q.krange[q];
+        gi += off * Q.kstride[q];
+      }
+    }
+    if (!in_range) {
+      raise_error(B.error, DERR_KEY_RANGE);
+      continue;
+    }
+#pragma unroll
+    for (int m = 0; m < kMaxMetrics; m++) {
+      if (m < nm) {
+        uint32_t a = extract(Q.xa[m], wstage, row, pw), v = a;
+        if (Q.mform[m] != MF_OPND) {
+          uint32_t b2 = extract(Q.xb[m], wstage, row, pw);
+          v = Q.mform[m] == MF_ADD ? a + b2 : Q.mform[m] == MF_SUB ? a - b2 : a * b2;
+        }
+        if (Q.nkeys == 0)
+          acc[m] += (long long)(int32_t)v;
+        else
+          atomicAdd(sums + m * G + gi, (unsigned long long)(long long)(int32_t)v);
+      }
+    }
+    if (Q.nkeys) sums[(size_t)nm * G + gi] = 1ull;  // the group has a row
+  }
+  if (Q.nkeys == 0) {
+#pragma unroll
+    for (int m = 0; m < kMaxMetrics; m++) {
+      if (m < nm) {
+        long long s = acc[m];
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0 && s) atomicAdd(sums + m, (unsigned long long)s);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kStarThreads, 2) batch_kernel(const __grid_constant__ BatchParams B) {
+  extern __shared__ __align__(128) uint8_t dyn[];
+  __shared__ uint64_t full[kStages], empty[kStages];
+  __shared__ long long stage_tile[kStages];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ncols = B.ncols, nst = B.nstages;
+  int32_t* ring = reinterpret_cast<int32_t*>(dyn);
+  WarpList* lists = reinterpret_cast<WarpList*>(dyn + (size_t)nst * ncols * kTileRows * 4);
+  if (tid == 0) {
+    for (int s = 0; s < nst; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kConsumerWarps);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+  const long long a0 = B.row_begin & ~3ll;
+  const long long end4 = (B.row_end + 3) & ~3ll;
+  const long long ntiles = (B.row_end - a0 + kTileRows - 1) / kTileRows;
+
+  if (warp == kConsumerWarps) {
+    if (lane == 0) {
+      long long issued = 0;
+      for (;; issued++) {
+        const int s = (int)(issued % nst);
+        const long long k = issued / nst;
+        if (k > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)((k - 1) & 1), kWaitPolls)) {
+          raise_error(B.error, DERR_TIMEOUT);
+          break;
+        }
+        const long long t = (long long)atomicAdd(B.tile_counter, 1ull);
+        if (t >= ntiles) {
+          stage_tile[s] = -1;  // end of the scan
+          mbar_arrive(&full[s]);
+          issued++;
+          break;
+        }
+        stage_tile[s] = t;
+        const long long start = a0 + t * kTileRows;
+        const long long stop = start + kTileRows < end4 ? start + kTileRows : end4;
+        const uint32_t bytes = (uint32_t)((stop - start) * 4);
+        mbar_arrive_expect_tx(&full[s], bytes * (uint32_t)ncols);
+        for (int c = 0; c < ncols; c++)
+          bulk_g2s(ring + ((size_t)s * ncols + c) * kTileRows, B.cols[c] + start, bytes, &full[s]);
+      }
+      const long long first = issued > nst ? issued - nst : 0;
+      for (long long q = first; q < issued; q++)
+        mbar_wait_bounded(&full[q % nst], (uint32_t)((q / nst) & 1), kWaitPolls);
+    }
+    return;
+  }
+  WarpList& L = lists[warp];
+  const uint32_t lt = lanemask_lt();
+  for (long long i = 0;; i++) {
+    const int s = (int)(i % nst);
+    if (!mbar_wait_bounded(&full[s], (uint32_t)((i / nst) & 1), kWaitPolls)) {
+      raise_error(B.error, DERR_TIMEOUT);
+      break;
+    }
+    const long long t = stage_tile[s];
+    if (t < 0) break;
+    const int32_t* wstage = ring + (size_t)s * ncols * kTileRows + warp * kWarpRows;
+    const long long slice_start = a0 + t * kTileRows + warp * kWarpRows;
+    for (int base = 0; base < B.nqueries; base += 32) {
+      const int q = base + lane;
+      bool act = false;
+      if (q < B.nqueries) {
+        const BatchQuery& Q = B.queries[q];
+        act = Q.row_begin < slice_start + kWarpRows && Q.row_end > slice_start;
+      }
+      uint32_t bq = __ballot_sync(0xffffffffu, act);
+      while (bq) {
+        const int qi = base + __ffs(bq) - 1;
+        bq &= bq - 1;
+        batch_query_slice(B.queries[qi], B, wstage, slice_start, L, lane, lt);
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
+}
+
+size_t batch_smem_bytes(const BatchParams& b) {
+  return (size_t)b.nstages * b.ncols * kTileRows * 4 + sizeof(WarpList) * kConsumerWarps;
+}
+
+int batch_grid_size(const BatchParams& b, size_t smem) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024);
+    attr = true;
+  }
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, kStarThreads, smem);
+  return num_sms() * (per_sm < 1 ? 1 : per_sm);
+}
+
+cudaError_t launch_batch(const BatchParams& b, int grid, size_t smem, cudaStream_t s) {
+  note_launch();
+  batch_kernel<<<grid, kStarThreads, smem, s>>>(b);
+  return cudaGetLastError();
+}
+
+// Groups of all queries numbered one after the other (BatchQuery::group_off).
+__device__ __forceinline__ int batch_query_of(const BatchQuery* Q, int nq, unsigned long long g) {
+  int lo = 0, hi = nq - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (Q[mid].group_off <= g)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void batch_flags_kernel(const BatchQuery* Q, int nq, const unsigned long long* slots,
+                                   unsigned long long total, uint32_t* flags) {
+  for (unsigned long long g = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; g < total;
+       g += (unsigned long long)gridDim.x * blockDim.x) {
+    const BatchQuery& q = Q[batch_query_of(Q, nq, g)];
+    const unsigned long long gi = g - q.group_off;
+    // A query without keys has exactly one result row.
+    flags[g] = q.nkeys == 0 ? 1u : (uint32_t)(slots[q.slot_off + (size_t)q.nmetrics * q.ngroups + gi] != 0ull);
+  }
+}
+
+__global__ void batch_write_kernel(const BatchQuery* Q, int nq, const unsigned long long* slots,
+                                   unsigned long long total, const uint32_t* flags, const unsigned long long* pos,
+                                   BatchOut o) {
+  for (unsigned long long g = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; g < total;
+       g += (unsigned long long)gridDim.x * blockDim.x) {
+    if (!flags[g]) continue;
+    const BatchQuery& q = Q[batch_query_of(Q, nq, g)];
+    const unsigned long long gi = g - q.group_off, at = pos[g];
+    for (int k = 0; k < q.nkeys; k++)
+      o.key[k][at] = (int32_t)((uint32_t)q.kmin[k] + (uint32_t)((gi / q.kstride[k]) % q.krange[k]));
+    for (int m = 0; m < q.nmetrics; m++) o.sum[m][at] = (long long)slots[q.slot_off + (size_t)m * q.ngroups + gi];
+  }
+}
+
+cudaError_t launch_batch_finalize(const BatchQuery* Q, int nq, const unsigned long long* slots,
+                                  unsigned long long total, uint32_t* flags, unsigned long long* pos,
+                                  unsigned long long* scan_tmp, const BatchOut* out, cudaStream_t s) {
+  const int grid = num_sms() * 4;
+  if (!out) {
+    note_launch();
+    batch_flags_kernel<<<grid, 256, 0, s>>>(Q, nq, slots, total, flags);
+    return launch_exclusive_scan(flags, total, pos, scan_tmp, s);
+  }
+  note_launch();
+  batch_write_kernel<<<grid, 256, 0, s>>>(Q, nq, slots, total, flags, pos, *out);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- finalize
 __global__ void group_flags_kernel(const unsigned long long* counts, unsigned long long G,
                                    uint32_t* flags) {

@@ -79,4 +79,19 @@ cudaError_t launch_finalize_dense(const StarParams& p, int32_t* const* key_out, 
                                   unsigned long long* scan_tmp, unsigned long long* out_count,
                                   cudaStream_t s);
 
+// ---- batched star queries (kern_star.cu)
+struct BatchOut {
+  int32_t* key[kMaxKeys];
+  long long* sum[kMaxMetrics];
+};
+size_t batch_smem_bytes(const BatchParams& b);
+int batch_grid_size(const BatchParams& b, size_t smem);
+cudaError_t launch_batch(const BatchParams& b, int grid, size_t smem, cudaStream_t s);
+// out == nullptr: flags (one per group of every query) and their exclusive
+// scan into pos (total + 1 entries); else write each flagged group's keys and
+// sums at pos into `out`.
+cudaError_t launch_batch_finalize(const BatchQuery* Q, int nq, const unsigned long long* slots,
+                                  unsigned long long total, uint32_t* flags, unsigned long long* pos,
+                                  unsigned long long* scan_tmp, const BatchOut* out, cudaStream_t s);
+
 }  // namespace svm

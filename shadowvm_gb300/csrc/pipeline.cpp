@@ -412,7 +412,21 @@ struct StepPlan {
   int order_class; // 0 filter/probe, 1 plain load
 };
 
-svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs) {
+// A planned fact pipeline: the kernel parameters (without scratch pointers)
+// and the result object's shape.
+struct StarPlan {
+  StarParams P{};
+  std::vector<int> fact_cols;   // StarParams::cols slot -> source column
+  std::vector<int> out_types;
+  int wide[kMaxMetrics] = {1, 1, 1};
+  int nkeys = 0, nmet = 0;
+  bool empty_src = false;       // the source has no bulk: empty result, no launch
+  bool empty_filter = false;    // a contradictory filter: no row passes
+  bool needs_prog = false;
+};
+
+svm_status plan_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs,
+                     StarPlan* plan) {
   std::string err;
   const int nkeys = (int)b.reduce_key.size();
   const int nmet = (int)b.metric_exp.size();
@@ -481,12 +495,14 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   // ---- the result object's shape
   std::vector<int> out_types(nkeys, SVM_INT32);
   for (int m = 0; m < nmet; m++) out_types.push_back(wide[m] ? SVM_INT64 : SVM_INT32);
+  plan->out_types = out_types;
+  plan->nkeys = nkeys;
+  plan->nmet = nmet;
+  for (int m = 0; m < nmet; m++) plan->wide[m] = wide[m];
   svm_status st;
   if (!src->has_bulks) {
     // No fact bulks: the reference runs no task and its sink stays empty.
-    ObjectPtr out = new_result_object(x, b.id, out_types, 0, &st);
-    if (st) return st;
-    x->objects[b.id] = out;
+    plan->empty_src = true;
     return SVM_OK;
   }
 
@@ -537,11 +553,12 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   }
 
   // ---- staged fact columns: every fact column the query reads
-  StarParams P{};
+  StarParams& P = plan->P;
+  P = StarParams{};
   P.error = x->d_error;
   P.row_begin = (long long)src->row0;
   P.row_end = (long long)(src->row0 + src->nrows);
-  std::vector<int> fact_cols;  // StarParams::cols slot -> fact column
+  std::vector<int>& fact_cols = plan->fact_cols;  // StarParams::cols slot -> fact column
   auto col_slot = [&](int c) {
     for (size_t i = 0; i < fact_cols.size(); i++)
       if (fact_cols[i] == c) return (int)i;
@@ -584,7 +601,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
     *pass = ov / w;
     return SVM_OK;
   };
-  std::vector<StepPlan> plan;
+  std::vector<StepPlan> order;
   std::set<int> ranged_done;
   for (int k = 1; k <= nref; k++) {
     if (join_of_obj[k] < 0) continue;
@@ -608,7 +625,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
       if ((st = range_pass(lc, r->second.first, r->second.second, &rp))) return st;
       sp.pass *= rp;
     }
-    plan.push_back(sp);
+    order.push_back(sp);
   }
   for (auto& kv : ranges) {
     if (ranged_done.count(kv.first)) continue;
@@ -619,16 +636,16 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
     sp.step.hi = kv.second.second;
     sp.cost = 0.25;
     if ((st = range_pass(kv.first, kv.second.first, kv.second.second, &sp.pass))) return st;
-    plan.push_back(sp);
+    order.push_back(sp);
   }
   // Independent filters: ascending cost / (1 - pass) minimises the expected
   // work per row.
-  std::stable_sort(plan.begin(), plan.end(), [](const StepPlan& a, const StepPlan& z) {
+  std::stable_sort(order.begin(), order.end(), [](const StepPlan& a, const StepPlan& z) {
     return a.cost / std::max(1e-6, 1.0 - a.pass) < z.cost / std::max(1e-6, 1.0 - z.pass);
   });
-  if ((int)plan.size() > kMaxSteps) return x->fail(SVM_E_UNSUPPORTED, "more than 8 filter steps");
-  P.nsteps = (int)plan.size();
-  for (size_t s = 0; s < plan.size(); s++) P.steps[s] = plan[s].step;
+  if ((int)order.size() > kMaxSteps) return x->fail(SVM_E_UNSUPPORTED, "more than 8 filter steps");
+  P.nsteps = (int)order.size();
+  for (size_t s = 0; s < order.size(); s++) P.steps[s] = order[s].step;
   auto operand_of = [&](const ColRef& r, Operand* o) -> bool {
     if (r.obj == 0) {
       *o = Operand{(int8_t)col_slot(r.col), -1};
@@ -712,6 +729,29 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   if ((int)fact_cols.size() > kMaxSteps) return x->fail(SVM_E_UNSUPPORTED, "query reads more than 8 fact columns");
   P.ncols = (int)fact_cols.size();
   for (size_t i = 0; i < fact_cols.size(); i++) P.cols[i] = (const int32_t*)src->base(fact_cols[i]);
+  plan->empty_filter = empty;
+  plan->needs_prog = P.npost > 0;
+  for (int m = 0; m < nmet; m++) plan->needs_prog |= P.metrics[m].form == MF_PROG;
+  flatten_plan(P);
+  return SVM_OK;
+}
+
+svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs) {
+  StarPlan plan;
+  svm_status st = plan_star(x, b, src, refs, &plan);
+  if (st) return st;
+  const std::vector<int>& out_types = plan.out_types;
+  const int nkeys = plan.nkeys, nmet = plan.nmet;
+  const int* wide = plan.wide;
+  if (plan.empty_src) {
+    ObjectPtr out = new_result_object(x, b.id, out_types, 0, &st);
+    if (st) return st;
+    x->objects[b.id] = out;
+    return SVM_OK;
+  }
+  StarParams& P = plan.P;
+  const unsigned long long G = P.ngroups;
+  const bool empty = plan.empty_filter;
 
   // ---- scratch: sums + counts (+ finalize buffers)
   x->scratch_reset();
@@ -729,7 +769,6 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   if (e) return x->cuda_fail(e, "cudaMemsetAsync");
   if (empty) P.row_end = P.row_begin;  // a contradictory filter: no row can pass
 
-  flatten_plan(P);
   // Ring depth: the most resident blocks per SM, then the deepest ring.
   int best_blocks = 0, best_st = 0;
   for (int nst = kStages; nst >= 2; nst--) {
@@ -801,29 +840,235 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
 
 }  // namespace
 
-svm_status run_pipeline(Ctx* x, const svm_pipeline* p) {
-  Bound b;
-  svm_status st = bind(x, p, &b);
+namespace {
+
+// Binds a pipeline and resolves its pre_pipeline_id objects.
+svm_status resolve(Ctx* x, const svm_pipeline* p, Bound* b, ObjectPtr* src, std::vector<ObjectPtr>* refs) {
+  svm_status st = bind(x, p, b);
   if (st) return st;
   if (p->npre < 1 || !p->pre_pipeline_id || !p->pre_pipeline_id[0])
-    return x->fail(SVM_E_INVALID_ARG, "pipeline " + b.id + " has no source object (pre_pipeline_id[0])");
+    return x->fail(SVM_E_INVALID_ARG, "pipeline " + b->id + " has no source object (pre_pipeline_id[0])");
   // service/service.cu:36-49: every pre_pipeline_id must name a cached object.
-  ObjectPtr src = x->find(p->pre_pipeline_id[0]);
-  if (!src) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + p->pre_pipeline_id[0]);
-  std::vector<ObjectPtr> refs;
+  *src = x->find(p->pre_pipeline_id[0]);
+  if (!*src) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + p->pre_pipeline_id[0]);
+  refs->clear();
   for (int i = 1; i < p->npre; i++) {
     ObjectPtr o = p->pre_pipeline_id[i] ? x->find(p->pre_pipeline_id[i]) : nullptr;
-    if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + (p->pre_pipeline_id[i] ? p->pre_pipeline_id[i] : "(null)"));
-    refs.push_back(o);
+    if (!o)
+      return x->fail(SVM_E_NOT_FOUND,
+                     std::string("no object ") + (p->pre_pipeline_id[i] ? p->pre_pipeline_id[i] : "(null)"));
+    refs->push_back(o);
   }
+  return SVM_OK;
+}
+
+struct BatchItem {
+  std::string id;
+  StarPlan plan;
+  ObjectPtr src;
+};
+
+// One batched launch over queries that share a fact table.
+svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
+  const int nq = (int)items.size();
+  // Union of the fact columns, identified by their storage.
+  std::vector<const void*> ucols;
+  auto uslot = [&](const void* base) {
+    for (size_t i = 0; i < ucols.size(); i++)
+      if (ucols[i] == base) return (int)i;
+    ucols.push_back(base);
+    return (int)ucols.size() - 1;
+  };
+  std::vector<BatchQuery> qs(nq);
+  unsigned long long slot_words = 0, total_groups = 0;
+  long long lo = LLONG_MAX, hi = LLONG_MIN;
+  for (int i = 0; i < nq; i++) {
+    StarPlan& pl = items[i].plan;
+    StarParams& P = pl.P;
+    BatchQuery& Q = qs[i];
+    std::vector<int> remap(pl.fact_cols.size());
+    for (size_t c = 0; c < pl.fact_cols.size(); c++) remap[c] = uslot(items[i].src->base(pl.fact_cols[c]));
+    Q.row_begin = P.row_begin;
+    Q.row_end = pl.empty_filter ? P.row_begin : P.row_end;
+    Q.nsteps = P.nsteps;
+    for (int k = 0; k < P.nsteps; k++) {
+      Q.steps[k] = P.steps[k];
+      Q.steps[k].col = remap[P.steps[k].col];
+      Q.steps[k].smem_word_off = -1;  // batch mode probes every table in global memory
+    }
+    auto fix = [&](Extract e) {
+      if (e.dim < 0) e.slot = remap[e.slot];
+      return e;
+    };
+    Q.nkeys = P.nkeys;
+    for (int k = 0; k < P.nkeys; k++) {
+      Q.kx[k] = fix(P.kx[k]);
+      Q.kmin[k] = P.kmin[k];
+      Q.krange[k] = P.krange[k];
+      Q.kstride[k] = (uint32_t)P.kstride[k];
+    }
+    Q.nmetrics = P.nmetrics;
+    for (int m = 0; m < P.nmetrics; m++) {
+      Q.mform[m] = P.metrics[m].form;
+      Q.xa[m] = fix(P.metrics[m].xa);
+      Q.xb[m] = fix(P.metrics[m].xb);
+    }
+    Q.ngroups = P.ngroups;
+    Q.slot_off = slot_words;
+    Q.group_off = total_groups;
+    slot_words += (unsigned long long)(P.nmetrics + 1) * P.ngroups;
+    total_groups += P.ngroups;
+    lo = std::min(lo, Q.row_begin);
+    hi = std::max(hi, Q.row_end);
+  }
+  if ((int)ucols.size() > kMaxBatchCols) return x->fail(SVM_E_UNSUPPORTED, "batch reads more than 12 fact columns");
+  if (hi < lo) hi = lo;
+  // Device buffers: the query table, group slots, the tile counter, finalize scratch.
+  x->scratch_reset();
+  const size_t qbytes = sizeof(BatchQuery) * nq;
+  const size_t fin_words = (total_groups + 1) / 2 + 1 + total_groups + 1 + scan_tmp_words(total_groups);
+  const size_t need = qbytes + 8 * slot_words + 8 + 8 * fin_words + 8 * 1024;
+  svm_status st = x->scratch_reserve(need);
+  if (st) return st;
+  void *dq, *slots, *ctr, *fin;
+  if ((st = x->scratch_take(qbytes, &dq)) || (st = x->scratch_take(8 * slot_words, &slots)) ||
+      (st = x->scratch_take(8, &ctr)) || (st = x->scratch_take(8 * fin_words, &fin)))
+    return st;
+  cudaError_t e = cudaMemcpyAsync(dq, qs.data(), qbytes, cudaMemcpyHostToDevice, x->stream);
+  if (!e) e = cudaMemsetAsync(slots, 0, 8 * slot_words, x->stream);
+  if (!e) e = cudaMemsetAsync(ctr, 0, 8, x->stream);
+  if (e) return x->cuda_fail(e, "batch setup");
+  BatchParams B{};
+  B.ncols = (int)ucols.size();
+  for (size_t c = 0; c < ucols.size(); c++) B.cols[c] = (const int32_t*)ucols[c];
+  B.row_begin = lo;
+  B.row_end = hi;
+  B.queries = (const BatchQuery*)dq;
+  B.nqueries = nq;
+  B.slots = (unsigned long long*)slots;
+  B.tile_counter = (unsigned long long*)ctr;
+  B.error = x->d_error;
+  // Ring depth: as deep as keeps two blocks per SM.
+  B.nstages = 2;
+  for (int nst = kStages; nst >= 2; nst--) {
+    B.nstages = nst;
+    if (batch_smem_bytes(B) <= 100 * 1024) break;
+  }
+  const size_t smem = batch_smem_bytes(B);
+  cudaEvent_t ev;
+  x->prof_begin(SVM_K_BATCH, &ev);
+  e = launch_batch(B, batch_grid_size(B, smem), smem, x->stream);
+  x->prof_end(SVM_K_BATCH, ev);
+  if (e) return x->cuda_fail(e, "batch kernel");
+  uint32_t* flags = (uint32_t*)fin;
+  unsigned long long* pos = (unsigned long long*)fin + (total_groups + 1) / 2 + 1;
+  unsigned long long* scant = pos + total_groups + 1;
+  x->prof_begin(SVM_K_FINALIZE, &ev);
+  e = launch_batch_finalize(B.queries, nq, B.slots, total_groups, flags, pos, scant, nullptr, x->stream);
+  x->prof_end(SVM_K_FINALIZE, ev);
+  std::vector<unsigned long long> hpos(total_groups + 1);
+  if (!e) e = cudaMemcpyAsync(hpos.data(), pos, 8 * (total_groups + 1), cudaMemcpyDeviceToHost, x->stream);
+  if (e) return x->cuda_fail(e, "batch finalize");
+  if ((st = sync_and_check(x, "batch"))) return st;
+  // One result store for the batch; each query's rows are a slice of it.
+  const unsigned long long rows = hpos[total_groups];
+  std::vector<int> types = {SVM_INT32, SVM_INT32, SVM_INT32, SVM_INT64, SVM_INT64, SVM_INT64};
+  ObjectPtr all = new_result_object(x, "", types, rows, &st);
+  if (st) return st;
+  BatchOut o{};
+  for (int k = 0; k < kMaxKeys; k++) o.key[k] = (int32_t*)all->col(k);
+  for (int m = 0; m < kMaxMetrics; m++) o.sum[m] = (long long*)all->col(kMaxKeys + m);
+  x->prof_begin(SVM_K_FINALIZE, &ev);
+  e = launch_batch_finalize(B.queries, nq, B.slots, total_groups, flags, pos, scant, &o, x->stream);
+  x->prof_end(SVM_K_FINALIZE, ev);
+  if (e) return x->cuda_fail(e, "batch write");
+  if ((st = sync_and_check(x, "batch write"))) return st;
+  for (int i = 0; i < nq; i++) {
+    const BatchQuery& Q = qs[i];
+    auto out = std::make_shared<Object>();
+    out->id = items[i].id;
+    out->version = x->next_version++;
+    out->ncols = Q.nkeys + Q.nmetrics;
+    out->types = items[i].plan.out_types;
+    for (int k = 0; k < Q.nkeys; k++) out->storage.push_back(all->storage[k]);
+    for (int m = 0; m < Q.nmetrics; m++) out->storage.push_back(all->storage[kMaxKeys + m]);
+    out->row0 = hpos[Q.group_off];
+    out->nrows = hpos[Q.group_off + Q.ngroups] - out->row0;
+    out->has_bulks = true;
+    out->bulk0_rows = out->nrows;
+    out->source_rows = out->nrows;
+    x->objects[items[i].id] = out;
+  }
+  return SVM_OK;
+}
+
+}  // namespace
+
+svm_status run_pipeline(Ctx* x, const svm_pipeline* p) {
+  Bound b;
+  ObjectPtr src;
+  std::vector<ObjectPtr> refs;
+  svm_status st = resolve(x, p, &b, &src, &refs);
+  if (st) return st;
   if (!b.is_reduce) return run_select(x, b, src);
   return run_star(x, b, src, refs);
 }
 
 svm_status run_batch(Ctx* x, int n, const svm_pipeline* p) {
+  // Select pipelines run first, in order (fact pipelines may join their outputs);
+  // reduce pipelines over the same fact table share one batched launch.  A
+  // batch in which some pipeline reads a reduce pipeline's output runs in order.
+  std::vector<char> reduce(n);
+  std::set<std::string> reduce_ids;
   for (int i = 0; i < n; i++) {
-    svm_status st = run_pipeline(x, &p[i]);
+    Bound b;
+    svm_status st = bind(x, &p[i], &b);
     if (st) return st;
+    reduce[i] = b.is_reduce;
+    if (b.is_reduce) reduce_ids.insert(b.id);
+  }
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < p[i].npre; j++)
+      if (p[i].pre_pipeline_id && p[i].pre_pipeline_id[j] && reduce_ids.count(p[i].pre_pipeline_id[j])) {
+        for (int k = 0; k < n; k++) {
+          svm_status st = run_pipeline(x, &p[k]);
+          if (st) return st;
+        }
+        return SVM_OK;
+      }
+  for (int i = 0; i < n; i++) {
+    svm_status st;
+    if (!reduce[i] && (st = run_pipeline(x, &p[i]))) return st;
+  }
+  std::map<const void*, std::vector<BatchItem>> groups;
+  for (int i = 0; i < n; i++) {
+    Bound b;
+    ObjectPtr src;
+    std::vector<ObjectPtr> refs;
+    svm_status st = resolve(x, &p[i], &b, &src, &refs);
+    if (st) return st;
+    if (!b.is_reduce) continue;
+    BatchItem it;
+    it.id = b.id;
+    it.src = src;
+    if ((st = plan_star(x, b, src, refs, &it.plan))) return st;
+    bool eligible = !it.plan.empty_src && !it.plan.needs_prog;
+    for (int m = 0; m < it.plan.nmet; m++) eligible &= it.plan.wide[m] != 0;
+    if (!eligible) {
+      if ((st = run_star(x, b, src, refs))) return st;
+      continue;
+    }
+    groups[src->storage[0].get()].push_back(std::move(it));
+  }
+  for (auto& g : groups) {
+    // Slot arrays and group numbering stay within 32-bit-friendly bounds per launch.
+    std::vector<BatchItem>& items = g.second;
+    for (size_t b0 = 0; b0 < items.size(); b0 += 1024) {
+      std::vector<BatchItem> part(std::make_move_iterator(items.begin() + b0),
+                                  std::make_move_iterator(items.begin() + std::min(items.size(), b0 + 1024)));
+      svm_status st = exec_batch(x, part);
+      if (st) return st;
+    }
   }
   return SVM_OK;
 }

@@ -162,6 +162,41 @@ struct StarParams {
   int* error;                       // device error word (division by zero, hash overflow)
 };
 
+// ---------------------------------------------------------------- batched star queries
+// Many fact pipelines over one resident fact table in one persistent launch:
+// the union of their fact columns is streamed once, and every query whose row
+// range covers a tile runs its own steps and aggregation on the staged tile.
+constexpr int kMaxBatchCols = 12;
+
+struct BatchQuery {                 // in device memory, one per query
+  long long row_begin, row_end;     // base rows this query reads
+  int nsteps;
+  Step steps[kMaxSteps];            // col = union column slot; tables in global memory
+  int nkeys;
+  Extract kx[kMaxKeys];
+  int32_t kmin[kMaxKeys];
+  uint32_t krange[kMaxKeys];
+  uint32_t kstride[kMaxKeys];
+  int nmetrics;
+  int mform[kMaxMetrics];
+  Extract xa[kMaxMetrics], xb[kMaxMetrics];
+  unsigned long long ngroups;
+  unsigned long long slot_off;      // sums at slots + slot_off, counts after nmetrics * ngroups
+  unsigned long long group_off;     // this query's first group in the batch's group numbering
+};
+
+struct BatchParams {
+  const int32_t* cols[kMaxBatchCols];
+  int ncols;
+  int nstages;
+  long long row_begin, row_end;     // union of the queries' ranges (base rows)
+  const BatchQuery* queries;
+  int nqueries;
+  unsigned long long* slots;
+  unsigned long long* tile_counter; // zeroed before the launch
+  int* error;
+};
+
 // Fills the flattened copies (Step table fields, Extract descriptors) from the
 // structured plan; called on the host once the plan is complete.
 inline Extract make_extract(const StarParams& P, Operand o, int32_t adjust) {

@@ -6,6 +6,8 @@ outputs and reducing (example/run_SSB_Q11.cu, run_SSB_Q31.cu).
   config 1  60 M-row fact, date + part join, GROUP BY (year, brand) SUM(revenue)
   config 2  600 M-row fact, date + customer + supplier join,
             GROUP BY (c_nation, s_nation, year) SUM(revenue - supplycost)
+  config 3  a batch of 256 queries shaped like configs 0-2 over views of the
+            resident 600 M-row config-2 fact table (make_batch)
 
 Every size can be scaled down for tests.  All columns are seeded and
 counter-based (datagen.py), so the fact table is generated on the device by
@@ -123,6 +125,135 @@ def make(config: int, *, fact_rows: int | None = None, seed: int = dg.DEFAULT_SE
     else:
         raise ValueError(f"no config {config}")
     return w
+
+
+# ------------------------------------------------------------------ batched queries
+_DATE_YEAR = None
+
+
+def _year_days(y0: int, y1: int) -> int:
+    global _DATE_YEAR
+    if _DATE_YEAR is None:
+        _DATE_YEAR = dg.date_table()["year"]
+    return int(np.count_nonzero((_DATE_YEAR >= y0) & (_DATE_YEAR <= y1)))
+
+
+def _u01(seed: int, stream: int) -> float:
+    return dg.draw(seed, stream, 0, (1 << 30) - 1) / float(1 << 30)
+
+
+@dataclass
+class BatchQuery:
+    shape: int                 # 0, 1, 2: shaped like configs 0, 1, 2
+    row0: int                  # the query reads fact rows [row0, row0 + nrows)
+    nrows: int
+    selectivity: float         # drawn target fraction of rows that pass
+    pipe: PipelineInfo
+    key_num: int
+
+
+@dataclass
+class BatchWorkload:
+    fact: Workload                                   # the config-2 fact table and its dimensions
+    dim_pipelines: list = field(default_factory=list)  # distinct dimension pipelines, shared
+    queries: list = field(default_factory=list)
+
+
+def make_batch(nq: int = 256, *, fact_rows: int | None = None, seed: int = dg.DEFAULT_SEED,
+               qseed: int | None = None, tuple_per_bulk: int | None = None, min_rows: int = 1_000_000,
+               n_part: int | None = None, n_cust: int | None = None, n_supp: int | None = None) -> BatchWorkload:
+    """`nq` seeded queries shaped like configs 0-2, each with its own predicate
+    constants, over the config-2 fact table (9 columns):
+
+      row range   log-uniform length in [min_rows, fact_rows], uniform start
+      selectivity log-uniform in [1e-4, 0.5]: a fact-side extprice window
+                  passes min(1, target / p) of the rows, p being the expected
+                  pass rate of the shape's own dimension and fact predicates
+
+    Fact rows are the view "lo_q<i>" of "lineorder"; dimension pipelines with
+    equal text are shared between queries."""
+    qs = seed if qseed is None else qseed
+    base = make(2, fact_rows=fact_rows, seed=seed, tuple_per_bulk=tuple_per_bulk, n_part=n_part,
+                n_cust=n_cust, n_supp=n_supp, qseed=qs)
+    pt = dg.part_table(base.n_part, seed)
+    base.dims["part"] = [pt["partkey"], pt["category"], pt["brand"]]
+    bw = BatchWorkload(base)
+    dims = {}
+
+    def dim(name, table, ncols, proj, pred):
+        if name not in dims:
+            dims[name] = dim_pipeline(name, table, int_schema(ncols), proj, pred)
+            bw.dim_pipelines.append(dims[name])
+        return name
+
+    n = base.fact_rows
+    lo_rows = max(1, min(min_rows, n))
+    ext_lo, ext_hi = dg.RANGES["extprice"]
+    schema = base.fact_schema()
+    for i in range(nq):
+        st = 10_000 + 16 * i
+        shape = dg.draw(qs, st, 0, 2)
+        length = int(round(np.exp(np.log(lo_rows) + _u01(qs, st + 1) * (np.log(n) - np.log(lo_rows)))))
+        length = max(1, min(n, length))
+        row0 = dg.draw(qs, st + 2, 0, n - length)
+        sel = float(np.exp(np.log(1e-4) + _u01(qs, st + 3) * (np.log(0.5) - np.log(1e-4))))
+        if shape == 0:
+            y, d, q = dg.draw(qs, st + 4, 1992, 1998), dg.draw(qs, st + 5, 0, 8), dg.draw(qs, st + 6, 20, 35)
+            p = _year_days(y, y) / dg.N_DATE * 3 / 11 * (q - 1) / 50
+            dims_used = [dim(f"b_date_y{y}", "date", 3, "$(0.0),$(0.1)", f"$(0.1)=={y}")]
+            joins = [("$(0.0)", "$(1.0)")]
+            keys, metric, key_num = "", "$(0.3)*$(0.2)", 0
+            pred = [f"$(0.2)>={d}", f"$(0.2)<={d + 2}", f"$(0.1)<{q}"]
+        elif shape == 1:
+            c = dg.draw(qs, st + 4, 0, 24)
+            p = 1 / 25
+            dims_used = [dim("b_date", "date", 3, "$(0.0),$(0.1)", None),
+                         dim(f"b_part_c{c}", "part", 3, "$(0.0),$(0.2)", f"$(0.1)=={c}")]
+            joins = [("$(0.0)", "$(1.0)"), ("$(0.4)", "$(2.0)")]
+            keys, metric, key_num = "$(1.1),$(2.1)", "$(0.7)", 2
+            pred = []
+        else:
+            r, r2, y = dg.draw(qs, st + 4, 0, 4), dg.draw(qs, st + 5, 0, 4), dg.draw(qs, st + 6, 1992, 1996)
+            p = _year_days(y, y + 2) / dg.N_DATE / 25
+            dims_used = [dim(f"b_date_w{y}", "date", 3, "$(0.0),$(0.1)", f"$(0.1)>={y} && $(0.1)<={y + 2}"),
+                         dim(f"b_cust_r{r}", "customer", 4, "$(0.0),$(0.2)", f"$(0.3)=={r}"),
+                         dim(f"b_supp_r{r2}", "supplier", 4, "$(0.0),$(0.2)", f"$(0.3)=={r2}")]
+            joins = [("$(0.0)", "$(1.0)"), ("$(0.5)", "$(2.0)"), ("$(0.6)", "$(3.0)")]
+            keys, metric, key_num = "$(2.1),$(3.1),$(1.1)", "$(0.7)-$(0.8)", 3
+            pred = []
+        frac = min(1.0, sel / p)
+        if frac < 1.0:
+            span = ext_hi - ext_lo + 1
+            width = max(1, int(round(frac * span)))
+            w0 = ext_lo + dg.draw(qs, st + 7, 0, span - width)
+            pred += [f"$(0.3)>={w0}", f"$(0.3)<={w0 + width - 1}"]
+        pipe = fact_pipeline(f"bq{i}", f"lo_q{i}", schema, dims_used, joins, keys, metric,
+                             predication=" && ".join(pred) or None)
+        bw.queries.append(BatchQuery(shape, row0, length, sel, pipe, key_num))
+    return bw
+
+
+def load_batch(engine, bw: BatchWorkload, generate_on_device: bool = True, build_dims: bool = True):
+    """Dimensions, the fact table, one view per query and (build_dims) the
+    shared dimension pipelines' outputs."""
+    load_engine(engine, bw.fact, generate_on_device=generate_on_device)
+    for i, q in enumerate(bw.queries):
+        engine.view(f"lo_q{i}", "lineorder", q.row0, q.nrows)
+    if build_dims:
+        for p in bw.dim_pipelines:
+            engine.run(p)
+
+
+def exact_batch_query(bw: BatchWorkload, i: int, fact: list | None = None):
+    """One query of the batch through the NumPy evaluator (oracle side)."""
+    from oracle import sql_exact
+    q = bw.queries[i]
+    objs = {name: list(cols) for name, cols in bw.fact.dims.items()}
+    for p in bw.dim_pipelines:
+        if p.id in q.pipe.pre_pipeline_id:
+            objs[p.id] = sql_exact.run_select(p, objs[p.pre_pipeline_id[0]])
+    f = bw.fact.fact_host(q.row0, q.nrows) if fact is None else [c[q.row0:q.row0 + q.nrows] for c in fact]
+    return sql_exact.run_reduce(q.pipe, f, [objs[x] for x in q.pipe.pre_pipeline_id[1:]])
 
 
 # ------------------------------------------------------------------ GPU side

@@ -1,0 +1,114 @@
+"""GPU parity of the batched path (svm_run_batch): many fact pipelines over
+views of one resident fact table in one persistent launch must give, query
+by query, exactly the results of running each pipeline alone (which the
+parity tests pin to the reference), and in EXACT mode the NumPy evaluation."""
+import numpy as np
+import pytest
+
+from shadowvm_gb300 import workloads as W
+from shadowvm_gb300.pipeline import dim_pipeline, fact_pipeline
+from shadowvm_gb300.proto import ValType
+
+pytestmark = pytest.mark.gpu
+
+SMALL = dict(fact_rows=3_000_000, min_rows=5_000, tuple_per_bulk=1_000_000, n_part=140_000,
+             n_cust=300_000, n_supp=20_000)
+
+
+def singles(eng, bw, idx=None):
+    out = {}
+    for i in (range(len(bw.queries)) if idx is None else idx):
+        q = bw.queries[i]
+        eng.run(q.pipe)
+        out[i] = eng.result(q.pipe.id, q.key_num)
+    return out
+
+
+def batched(eng, bw, idx=None):
+    idx = list(range(len(bw.queries))) if idx is None else idx
+    eng.run_batch([bw.queries[i].pipe for i in idx])
+    return {i: eng.result(bw.queries[i].pipe.id, bw.queries[i].key_num) for i in idx}
+
+
+@pytest.mark.parametrize("mode", ["ref_compat", "exact"])
+def test_batch_equals_one_launch_per_query(engine_factory, mode):
+    bw = W.make_batch(64, qseed=11, **SMALL)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, join_mode=mode)
+    W.load_batch(eng, bw)
+    one = singles(eng, bw)
+    n0 = eng.kernel_launches()
+    many = batched(eng, bw)
+    launches = eng.kernel_launches() - n0
+    assert launches < 10, launches  # one scan kernel plus the finalize kernels
+    nonempty = 0
+    for i in one:
+        np.testing.assert_array_equal(many[i][0], one[i][0], err_msg=f"keys of query {i}")
+        np.testing.assert_array_equal(many[i][1], one[i][1], err_msg=f"sums of query {i}")
+        nonempty += len(one[i][1]) > 0 and np.any(one[i][1] != 0)
+    assert nonempty > 32
+
+
+def test_batch_exact_equals_numpy(engine_factory):
+    bw = W.make_batch(24, qseed=5, **SMALL)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, join_mode="exact")
+    W.load_batch(eng, bw)
+    got = batched(eng, bw)
+    fact = bw.fact.fact_host(0, bw.fact.fact_rows)
+    for i in range(len(bw.queries)):
+        ek, es = W.exact_batch_query(bw, i, fact)
+        np.testing.assert_array_equal(got[i][0], ek, err_msg=f"keys of query {i}")
+        np.testing.assert_array_equal(got[i][1], es, err_msg=f"sums of query {i}")
+
+
+def test_batch_mixed_with_selects_and_unbatchable(engine_factory):
+    """Dimension pipelines in the same batch run first; a pipeline the batch
+    kernel does not take (int32 sums, a division) runs alone; empty filters
+    and empty views keep their single-query results."""
+    bw = W.make_batch(12, qseed=3, **SMALL)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk)
+    W.load_batch(eng, bw, build_dims=False)
+    schema = bw.fact.fact_schema()
+    extra = [
+        fact_pipeline("x_int32", "lo_q0", schema, ["b_date"], [("$(0.0)", "$(1.0)")], "$(1.1)", "$(0.1)",
+                      metric_type=ValType.Int32),
+        fact_pipeline("x_div", "lo_q1", schema, ["b_date"], [("$(0.0)", "$(1.0)")], "$(1.1)", "$(0.7)/7"),
+        fact_pipeline("x_empty", "lo_q2", schema, ["b_date"], [("$(0.0)", "$(1.0)")], "$(1.1)", "$(0.7)",
+                      predication="$(0.1)>60"),
+        fact_pipeline("x_scalar", "lo_q3", schema, [], [], "", "$(0.7)+$(0.8)",
+                      predication="$(0.2)==4"),
+    ]
+    eng.view("lo_none", "lineorder", 10, 0)
+    extra.append(fact_pipeline("x_none", "lo_none", schema, ["b_date"], [("$(0.0)", "$(1.0)")], "$(1.1)",
+                               "$(0.7)"))
+    if not any(p.id == "b_date" for p in bw.dim_pipelines):
+        bw.dim_pipelines.append(dim_pipeline("b_date", "date", W.int_schema(3), "$(0.0),$(0.1)", None))
+    pipes = list(bw.dim_pipelines) + [q.pipe for q in bw.queries] + extra
+    eng.run_batch(pipes)
+    facts = pipes[len(bw.dim_pipelines):]
+    nkeys = {p.id: len([k for k in p.workflow[-2].args["dim"].split(",") if k]) for p in facts}
+    got = {p.id: eng.result(p.id, nkeys[p.id]) for p in facts}
+    for p in facts:
+        eng.run(p)
+        k, s = eng.result(p.id, nkeys[p.id])
+        np.testing.assert_array_equal(got[p.id][0], k, err_msg=p.id)
+        np.testing.assert_array_equal(got[p.id][1], s, err_msg=p.id)
+    assert got["x_empty"][1].shape[0] == 0
+    assert got["x_none"][1].shape[0] == 0
+    assert got["x_scalar"][1].shape == (1, 1)
+
+
+def test_batch_full_range_and_overlaps(engine_factory):
+    """Queries whose ranges start and end mid-tile, coincide, nest and cover
+    the whole table, including one-row views."""
+    bw = W.make_batch(8, qseed=9, **SMALL)
+    n = bw.fact.fact_rows
+    spans = [(0, n), (0, n), (1, n - 1), (1023, 1), (1024, 1025), (n - 1, 1), (777, 3_333), (5, 2_000_000)]
+    for q, (r0, ln) in zip(bw.queries, spans):
+        q.row0, q.nrows = r0, ln
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk)
+    W.load_batch(eng, bw)
+    one = singles(eng, bw)
+    many = batched(eng, bw)
+    for i in one:
+        np.testing.assert_array_equal(many[i][0], one[i][0])
+        np.testing.assert_array_equal(many[i][1], one[i][1])
