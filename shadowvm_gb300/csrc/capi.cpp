@@ -178,6 +178,7 @@ void svm_destroy(svm_ctx* c) {
   if (x->stream) cudaStreamSynchronize(x->stream);
   x->prof_collect();
   x->objects.clear();
+  x->merged_cache.clear();
   x->dim_cache.clear();
   x->scratch.reset();
   for (auto e : x->event_pool) cudaEventDestroy(e);
@@ -354,6 +355,7 @@ svm_status svm_object_drop(svm_ctx* c, const char* id) {
   cudaStreamSynchronize(x->stream);
   x->objects.erase(it);
   // Tables built over the dropped object are keyed by its version; drop them too.
+  x->merged_cache.clear();
   for (auto d = x->dim_cache.begin(); d != x->dim_cache.end();) {
     if (d->first.compare(0, std::strlen(id) + 1, std::string(id) + "#") == 0)
       d = x->dim_cache.erase(d);

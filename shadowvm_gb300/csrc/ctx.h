@@ -71,6 +71,13 @@ struct DimTable {
 };
 using DimTablePtr = std::shared_ptr<DimTable>;
 
+// A merged probe table of the batch path, kept while its source tables live.
+struct MergedTable {
+  DevBufPtr buf;
+  std::vector<DimTablePtr> srcs;
+  unsigned long long stamp = 0;
+};
+
 struct ProfEvent {
   int cls;
   cudaEvent_t a, b;
@@ -86,6 +93,8 @@ struct Ctx {
   unsigned long long next_version = 1;
   std::map<std::string, ObjectPtr> objects;
   std::map<std::string, DimTablePtr> dim_cache;
+  std::map<std::string, MergedTable> merged_cache;
+  unsigned long long merged_stamp = 0;
   int* d_error = nullptr;                     // device error word
   // Grow-only scratch arena, carved per operation.
   DevBufPtr scratch;

@@ -1,0 +1,419 @@
+// Batched star queries with merged probe tables.
+//
+// One persistent block per SM scans the union of a batch's fact columns once
+// (bulk-copy ring, dynamic tile hand-out).  For every 1024-row tile the block
+// first looks every row up once in each merged probe table the tile's queries
+// need (ProbeGroup: the dense dimension tables probed through one fact column,
+// concatenated per key), keeps the merged words in shared memory and turns
+// each needed table's present bits into a 1024-bit row bitmap with warp
+// ballots.  Then its warps take the tile's queries one at a time (the next
+// query's descriptor is copied in while one runs).  A query's probe steps are
+// one AND of a bitmap word per lane; its range steps test staged fact values,
+// with ballots over every row while many rows live, else only the live rows;
+// only its surviving rows reach the int64 group slots.  The lookups are thus
+// shared by every query of the batch, and a query's work per tile is a few
+// instructions per 32 rows.
+#include <climits>
+
+#include "kern_common.cuh"
+#include "kernels.h"
+
+namespace svm {
+namespace {
+
+constexpr int kMBThreads = (kMBatchWarps + 1) * 32;
+constexpr int kMBConsumers = kMBatchWarps * 32;
+constexpr uint32_t kPolls = 1u << 22;
+
+__device__ __forceinline__ void consumer_bar() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kMBConsumers) : "memory");
+}
+
+__device__ __forceinline__ uint32_t lane_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+constexpr int kChunks = kTileRows / 32;     // bitmap words per tile
+constexpr int kBmStride = kChunks + 1;      // a table's bitmap row, padded (conflict-free stores)
+constexpr int kDescChunks = (int)(sizeof(MQuery) / 16);
+constexpr int kDenseRows = 256;             // live rows above which a range test runs on every row
+static_assert(sizeof(MQuery) % 16 == 0 && kDescChunks <= 32, "MQuery is copied in 16-byte pieces by one warp");
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// A value for the aggregation: a staged fact value, or a payload field of a
+// merged probe word (optionally a row index into `col`), plus `base`.
+__device__ __forceinline__ uint32_t mx(const MExtract& x, const int32_t* stage, const uint32_t* mw, int row) {
+  if (x.src < 0) return (uint32_t)stage[x.slot * kTileRows + row] + (uint32_t)x.base;
+  uint32_t v = (mw[x.src * kTileRows + row] >> x.shift) & x.mask;
+  if (x.col) v = (uint32_t)__ldg(x.col + v);
+  return v + (uint32_t)x.base;
+}
+
+// Looks one 32-row chunk up in a merged table (lane = row of the chunk), keeps
+// the row's merged words and returns word 0 (the present bits).
+template <int W>
+__device__ __forceinline__ uint32_t fill_row(const ProbeGroup& G, const int32_t* stage, uint32_t* mw, int row) {
+  const uint32_t off = (uint32_t)stage[G.col * kTileRows + row] - (uint32_t)G.key_min;
+  const bool in = off < G.span;
+  const uint32_t* src = G.table + (size_t)(in ? off : 0u) * W;
+  uint32_t v[W];
+  if (W == 1) {
+    v[0] = in ? __ldg(src) : 0u;
+  } else if (W == 2) {
+    const uint2 a = in ? __ldg(reinterpret_cast<const uint2*>(src)) : make_uint2(0u, 0u);
+    v[0] = a.x;
+    v[1 % W] = a.y;
+  } else {
+#pragma unroll
+    for (int h = 0; h < W / 4; h++) {
+      const uint4 a = in ? __ldg(reinterpret_cast<const uint4*>(src) + h) : make_uint4(0u, 0u, 0u, 0u);
+      v[(4 * h + 0) % W] = a.x;
+      v[(4 * h + 1) % W] = a.y;
+      v[(4 * h + 2) % W] = a.z;
+      v[(4 * h + 3) % W] = a.w;
+    }
+  }
+#pragma unroll
+  for (int w = 0; w < W; w++) mw[(G.word_off + w) * kTileRows + row] = v[w];
+  return v[0];
+}
+
+// 32 x 32 bit transpose across a warp: lane i holds row i on entry (bit j =
+// element (i, j)) and column i on return (bit j = element (j, i)).  Five
+// exchange steps, each swapping the off-diagonal blocks of half the size.
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
+  const uint32_t masks[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+  for (int k = 0; k < 5; k++) {
+    const int s = 16 >> k;
+    const uint32_t m = masks[k];
+    const uint32_t y = __shfl_xor_sync(0xffffffffu, x, s);
+    x = (lane & s) ? ((x & ~m) | ((y & ~m) >> s)) : ((x & m) | ((y & m) << s));
+  }
+  return x;
+}
+
+// One query over one staged tile (local rows [lo, hi)).  Lane L owns rows
+// [32 L, 32 L + 32) as the bits of one mask word.
+__device__ __forceinline__ void mquery_tile(const MQuery& Q, const BatchParams& B, const int32_t* stage,
+                                            const uint32_t* mw, const uint32_t* bm, int lo, int hi, int lane) {
+  const int r0 = 32 * lane;
+  const int a = lo - r0 > 0 ? lo - r0 : 0, b = hi - r0 < 32 ? hi - r0 : 32;
+  uint32_t m = a >= b ? 0u : (b - a == 32 ? 0xFFFFFFFFu : ((1u << (b - a)) - 1u) << a);
+  const int np = Q.nprobe, nr = Q.nrange;
+  for (int p = 0; p < np; p++) m &= bm[Q.probe_tab[p] * kBmStride + lane];
+  for (int r = 0; r < nr; r++) {
+    const int live = __reduce_add_sync(0xffffffffu, __popc(m));
+    if (!live) return;
+    const MRange R = Q.range[r];
+    const int32_t* cv = stage + R.col * kTileRows;
+    const uint32_t span = (uint32_t)R.hi - (uint32_t)R.lo;
+    if (live > kDenseRows) {
+      uint32_t keep = 0;
+#pragma unroll 8
+      for (int i = 0; i < kChunks; i++) {
+        const uint32_t bb = __ballot_sync(0xffffffffu, (uint32_t)cv[32 * i + lane] - (uint32_t)R.lo <= span);
+        keep = lane == i ? bb : keep;
+      }
+      m &= keep;
+    } else {
+      for (uint32_t bb = m; bb; bb &= bb - 1) {
+        const int j = __ffs(bb) - 1;
+        if ((uint32_t)cv[r0 + j] - (uint32_t)R.lo > span) m &= ~(1u << j);
+      }
+    }
+  }
+  if (!__any_sync(0xffffffffu, m)) return;
+  const int nkeys = Q.nkeys, nm = Q.nmetrics;
+  unsigned long long* sums = B.slots + Q.slot_off;
+  const unsigned long long G = Q.ngroups;
+  // The keys' operands, read once per query and tile (the metrics' stay in
+  // the shared-memory descriptor).
+  MExtract kx[kMaxKeys];
+  uint32_t kr[kMaxKeys], ks[kMaxKeys];
+#pragma unroll
+  for (int q = 0; q < kMaxKeys; q++) {
+    kx[q] = Q.kx[q];
+    kr[q] = Q.krange[q];
+    ks[q] = Q.kstride[q];
+  }
+  const MExtract* xa = Q.xa;
+  const MExtract* xb = Q.xb;
+  const uint8_t* mf = Q.mform;
+  long long acc[kMaxMetrics] = {0, 0, 0};
+  for (uint32_t bb = m; bb; bb &= bb - 1) {
+    const int row = r0 + __ffs(bb) - 1;
+    uint32_t gi = 0;
+    bool in_range = true;
+#pragma unroll
+    for (int q = 0; q < kMaxKeys; q++) {
+      if (q < nkeys) {
+        const uint32_t off = mx(kx[q], stage, mw, row);
+        in_range &= off < kr[q];
+        gi += off * ks[q];
+      }
+    }
+    if (!in_range) {
+      raise_error(B.error, DERR_KEY_RANGE);
+      continue;
+    }
+#pragma unroll
+    for (int mi = 0; mi < kMaxMetrics; mi++) {
+      if (mi < nm) {
+        const uint32_t va = mx(xa[mi], stage, mw, row);
+        uint32_t v = va;
+        const int f = mf[mi];
+        if (f != MF_OPND) {
+          const uint32_t vb = mx(xb[mi], stage, mw, row);
+          v = f == MF_ADD ? va + vb : f == MF_SUB ? va - vb : va * vb;
+        }
+        if (nkeys == 0)
+          acc[mi] += (long long)(int32_t)v;
+        else
+          atomicAdd(sums + (size_t)mi * G + gi, (unsigned long long)(long long)(int32_t)v);
+      }
+    }
+    if (nkeys) sums[(size_t)nm * G + gi] = 1ull;  // the group has a row
+  }
+  if (nkeys == 0) {
+#pragma unroll
+    for (int mi = 0; mi < kMaxMetrics; mi++) {
+      if (mi < nm) {
+        long long sacc = acc[mi];
+        for (int o = 16; o; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+        if (lane == 0 && sacc) atomicAdd(sums + mi, (unsigned long long)sacc);
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void copy_desc(MQuery* dst, const MQuery* src, int lane) {
+  if (lane < kDescChunks)
+    cp_async16(reinterpret_cast<uint4*>(dst) + lane, reinterpret_cast<const uint4*>(src) + lane);
+  cp_async_commit();
+}
+
+__global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_constant__ BatchParams B) {
+  extern __shared__ __align__(128) uint8_t dyn[];
+  __shared__ uint64_t full[kStages], empty[kStages];
+  __shared__ long long stage_tile[kStages];
+  __shared__ long long s_tile;
+  __shared__ int s_next;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ncols = B.ncols, nst = B.nstages, nq = B.nqueries;
+  int32_t* ring = reinterpret_cast<int32_t*>(dyn);
+  uint32_t* mw = reinterpret_cast<uint32_t*>(dyn + (size_t)nst * ncols * kTileRows * 4);
+  uint32_t* bm = mw + (size_t)B.nmwords * kTileRows;
+  MQuery* dbuf = reinterpret_cast<MQuery*>(bm + kMaxMergedTables * kBmStride);
+  long long* qlo = reinterpret_cast<long long*>(dbuf + 2 * kMBatchWarps);
+  long long* qhi = qlo + nq;
+  uint32_t* qg = reinterpret_cast<uint32_t*>(qhi + nq);
+  uint16_t* act = reinterpret_cast<uint16_t*>(qg + nq);
+  if (tid == 0) {
+    for (int s = 0; s < nst; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_fence_init();
+  }
+  for (int q = tid; q < nq; q += kMBThreads) {
+    qlo[q] = B.mq[q].row_begin;
+    qhi[q] = B.mq[q].row_end;
+    qg[q] = B.mq[q].gmask;
+  }
+  __syncthreads();
+  const long long a0 = B.row_begin & ~3ll;
+  const long long end4 = (B.row_end + 3) & ~3ll;
+  const long long ntiles = (B.row_end - a0 + kTileRows - 1) / kTileRows;
+
+  if (warp == kMBatchWarps) {
+    // Producer: one thread hands out tiles and issues their bulk copies.
+    if (lane == 0) {
+      long long issued = 0;
+      for (;; issued++) {
+        const int s = (int)(issued % nst);
+        const long long k = issued / nst;
+        if (k > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)((k - 1) & 1), kPolls)) {
+          raise_error(B.error, DERR_TIMEOUT);
+          break;
+        }
+        const long long t = (long long)atomicAdd(B.tile_counter, 1ull);
+        if (t >= ntiles) {
+          stage_tile[s] = -1;  // end of the scan
+          mbar_arrive(&full[s]);
+          issued++;
+          break;
+        }
+        stage_tile[s] = t;
+        const long long start = a0 + t * kTileRows;
+        const long long stop = start + kTileRows < end4 ? start + kTileRows : end4;
+        const uint32_t bytes = (uint32_t)((stop - start) * 4);
+        mbar_arrive_expect_tx(&full[s], bytes * (uint32_t)ncols);
+        for (int c = 0; c < ncols; c++)
+          bulk_g2s(ring + ((size_t)s * ncols + c) * kTileRows, B.cols[c] + start, bytes, &full[s]);
+      }
+      // Every copy issued lands before the block may exit.
+      const long long first = issued > nst ? issued - nst : 0;
+      for (long long q = first; q < issued; q++)
+        mbar_wait_bounded(&full[q % nst], (uint32_t)((q / nst) & 1), kPolls);
+    }
+    return;
+  }
+
+  const uint32_t lt = lane_lt();
+  MQuery* mybuf = dbuf + 2 * warp;
+  for (long long i = 0;; i++) {
+    const int s = (int)(i % nst);
+    const uint32_t parity = (uint32_t)((i / nst) & 1);
+    if (tid == 0) {
+      s_tile = mbar_wait_bounded(&full[s], parity, kPolls) ? stage_tile[s] : -2;
+      s_next = 0;
+    }
+    consumer_bar();
+    const long long t = s_tile;
+    if (t < 0) {
+      if (t == -2 && tid == 0) raise_error(B.error, DERR_TIMEOUT);
+      break;
+    }
+    if (tid != 0) mbar_wait_bounded(&full[s], parity, kPolls);  // completes at once: acquires the copies
+    const int32_t* stage = ring + (size_t)s * ncols * kTileRows;
+    const long long tile_start = a0 + t * kTileRows, tile_end = tile_start + kTileRows;
+    // The tile's queries (warp 0 lists them) and the probe groups they need.
+    uint32_t need = 0;
+    int na = 0;
+    for (int base = 0; base < nq; base += 32) {
+      const int q = base + lane;
+      const bool a = q < nq && qlo[q] < tile_end && qhi[q] > tile_start;
+      if (a) need |= qg[q];
+      const uint32_t bq = __ballot_sync(0xffffffffu, a);
+      if (warp == 0 && a) act[na + __popc(bq & lt)] = (uint16_t)q;
+      na += __popc(bq);
+    }
+    need = __reduce_or_sync(0xffffffffu, need);
+    // Merged words of every row; the present bits, transposed, give each
+    // table's row bitmap.
+    const int ng = __popc(need);
+    for (int it = warp; it < ng * kChunks; it += kMBatchWarps) {
+      const int gsel = it / kChunks, chunk = it % kChunks;
+      uint32_t mm = need;
+      for (int z = 0; z < gsel; z++) mm &= mm - 1;
+      const int g = __ffs(mm) - 1;
+      const ProbeGroup& G = B.probe[g];
+      const int row = chunk * 32 + lane;
+      uint32_t present;
+      switch (G.words) {
+        case 1: present = fill_row<1>(G, stage, mw, row); break;
+        case 2: present = fill_row<2>(G, stage, mw, row); break;
+        case 4: present = fill_row<4>(G, stage, mw, row); break;
+        default: present = fill_row<8>(G, stage, mw, row); break;
+      }
+      present = transpose32(present, lane);
+      const int t0 = B.gtab0[g];
+      if (lane < B.gtab0[g + 1] - t0) bm[(t0 + lane) * kBmStride + chunk] = present;
+    }
+    consumer_bar();
+    // Queries, claimed one at a time; the next one's descriptor is copied while
+    // this one runs.
+    int k = 0;
+    if (lane == 0) k = atomicAdd(&s_next, 1);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k < na) copy_desc(mybuf, B.mq + act[k], lane);
+    int cur = 0;
+    while (k < na) {
+      int kn = 0;
+      if (lane == 0) kn = atomicAdd(&s_next, 1);
+      kn = __shfl_sync(0xffffffffu, kn, 0);
+      if (kn < na)
+        copy_desc(mybuf + (cur ^ 1), B.mq + act[kn], lane);
+      else
+        cp_async_commit();
+      cp_async_wait<1>();
+      __syncwarp();
+      const int q = act[k];
+      const long long lo = qlo[q] > tile_start ? qlo[q] - tile_start : 0;
+      const long long hi = qhi[q] < tile_end ? qhi[q] - tile_start : kTileRows;
+      mquery_tile(mybuf[cur], B, stage, mw, bm, (int)lo, (int)hi, lane);
+      __syncwarp();
+      cur ^= 1;
+      k = kn;
+    }
+    cp_async_wait<0>();
+    consumer_bar();
+    if (tid == 0) mbar_arrive(&empty[s]);
+  }
+}
+
+__global__ void merge_build_kernel(const __grid_constant__ MergeBuild M, uint32_t* out) {
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < M.span;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    uint32_t w[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+    for (int i = 0; i < M.nsrc; i++) {
+      const MergeSrc& S = M.src[i];
+      const long long idx = (long long)M.key_min + (long long)k - (long long)S.key_min;
+      if (idx < 0 || idx >= (long long)S.span) continue;
+      const unsigned long long bit = (unsigned long long)idx * (unsigned)S.entry_bits;
+      uint32_t e = S.words[bit >> 5] >> (bit & 31);
+      if (S.entry_bits < 32) e &= (1u << S.entry_bits) - 1u;
+      w[0] |= (e & 1u) << S.present_bit;
+      const uint32_t pay = e >> 1;
+#pragma unroll
+      for (int z = 0; z < 8; z++)
+        if (z == S.pay_word && S.entry_bits > 1) w[z] |= pay << S.pay_bit;
+    }
+    for (int z = 0; z < M.words; z++) out[k * M.words + z] = w[z];
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_merge_build(const MergeBuild& m, uint32_t* out, cudaStream_t s) {
+  if (m.span == 0) return cudaSuccess;
+  unsigned long long blocks = (m.span + 255) / 256;
+  const unsigned long long cap = (unsigned long long)num_sms() * 8;
+  note_launch();
+  merge_build_kernel<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(m, out);
+  return cudaGetLastError();
+}
+
+size_t mbatch_smem_bytes(const BatchParams& b) {
+  return (size_t)b.nstages * b.ncols * kTileRows * 4 + (size_t)b.nmwords * kTileRows * 4 +
+         (size_t)kMaxMergedTables * kBmStride * 4 + sizeof(MQuery) * 2 * kMBatchWarps +
+         (size_t)b.nqueries * (8 + 8 + 4 + 2) + 16;
+}
+
+int mbatch_grid_size(const BatchParams& b, size_t smem) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(mbatch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    attr = true;
+  }
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mbatch_kernel, kMBThreads, smem);
+  return num_sms() * per_sm;
+}
+
+void mbatch_attributes(int* regs, int* max_threads, size_t* static_smem) {
+  cudaFuncAttributes a{};
+  cudaFuncGetAttributes(&a, mbatch_kernel);
+  *regs = a.numRegs;
+  *max_threads = a.maxThreadsPerBlock;
+  *static_smem = a.sharedSizeBytes;
+}
+
+cudaError_t launch_mbatch(const BatchParams& b, int grid, size_t smem, cudaStream_t s) {
+  note_launch();
+  mbatch_kernel<<<grid, kMBThreads, smem, s>>>(b);
+  return cudaGetLastError();
+}
+
+}  // namespace svm

@@ -94,4 +94,11 @@ cudaError_t launch_batch_finalize(const BatchQuery* Q, int nq, const unsigned lo
                                   unsigned long long total, uint32_t* flags, unsigned long long* pos,
                                   unsigned long long* scan_tmp, const BatchOut* out, cudaStream_t s);
 
+// ---- merged-probe batch (kern_mbatch.cu)
+cudaError_t launch_merge_build(const MergeBuild& m, uint32_t* out, cudaStream_t s);
+size_t mbatch_smem_bytes(const BatchParams& b);
+int mbatch_grid_size(const BatchParams& b, size_t smem);  // 0: the block does not fit an SM
+void mbatch_attributes(int* regs, int* max_threads, size_t* static_smem);
+cudaError_t launch_mbatch(const BatchParams& b, int grid, size_t smem, cudaStream_t s);
+
 }  // namespace svm

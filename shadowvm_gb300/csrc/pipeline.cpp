@@ -423,6 +423,7 @@ struct StarPlan {
   bool empty_src = false;       // the source has no bulk: empty result, no launch
   bool empty_filter = false;    // a contradictory filter: no row passes
   bool needs_prog = false;
+  std::vector<DimTablePtr> dim_tables;  // per StarParams dim
 };
 
 svm_status plan_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs,
@@ -586,6 +587,9 @@ svm_status plan_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::ve
     smem_words += (int)((bs.first / 4 + 3) & ~size_t(3));
   }
   P.smem_table_words = smem_words;
+  plan->dim_tables.assign(ndims, nullptr);
+  for (int k = 1; k <= nref; k++)
+    if (dim_of_obj[k] >= 0) plan->dim_tables[dim_of_obj[k]] = tables[k];
   // ---- filter steps: probes (a range on the same column folded in) and ranges
   struct StepPlan {
     Step step;
@@ -868,7 +872,173 @@ struct BatchItem {
   ObjectPtr src;
 };
 
-// One batched launch over queries that share a fact table.
+// Merged probe tables for a batch: the dense tables probed through each fact
+// column, at most 32 per group.  Word 0 of a merged entry holds the group's
+// present bits from bit 0 up; payloads (entry >> 1) go first-fit, widest
+// first, into the top of word 0 and then into words 1..7.  At most
+// kMaxMergedWords words per row and kMaxMergedTables table slots per batch.
+struct MergePlan {
+  struct Place {
+    int group = -1, slot = -1, present_bit = 0, pay_word = 0, pay_bit = 0;
+  };
+  std::map<std::pair<int, const DimTable*>, Place> place;  // (union column, table) -> placement
+  std::vector<ProbeGroup> groups;
+  std::vector<std::vector<std::pair<DimTablePtr, Place>>> members;
+  int nmwords = 0;
+  std::vector<int> gtab0;                  // group g owns table slots [gtab0[g], gtab0[g + 1])
+};
+
+void plan_merge(const std::vector<BatchQuery>& qs, const std::vector<BatchItem>& items, MergePlan* mp) {
+  std::vector<int> col_order;
+  std::map<int, std::vector<DimTablePtr>> by_col;
+  for (size_t i = 0; i < qs.size(); i++)
+    for (int k = 0; k < qs[i].nsteps; k++) {
+      const Step& st = qs[i].steps[k];
+      if (st.kind != STEP_PROBE) continue;
+      const DimTablePtr& T = items[i].plan.dim_tables[st.dim];
+      if (T->desc.layout != LAYOUT_DENSE) continue;
+      auto& v = by_col[st.col];
+      if (v.empty()) col_order.push_back(st.col);
+      if (std::find(v.begin(), v.end(), T) == v.end()) v.push_back(T);
+    }
+  for (int col : col_order) {
+    std::vector<DimTablePtr> tabs = by_col[col];
+    std::stable_sort(tabs.begin(), tabs.end(), [](const DimTablePtr& a, const DimTablePtr& z) {
+      return a->desc.entry_bits > z->desc.entry_bits;
+    });
+    size_t next = 0;
+    while (next < tabs.size() && (int)mp->groups.size() < kMaxProbeGroups) {
+      // A group takes the column's next tables while their present bits,
+      // payloads (8 words) and key span fit; its present region is reserved first.
+      const int reserve = (int)std::min<size_t>(32, tabs.size() - next);
+      const int g = (int)mp->groups.size();
+      mp->groups.push_back(ProbeGroup{col, 1, 0, 0, 0, nullptr});
+      mp->members.emplace_back();
+      int ntab = 0, low0 = 32;
+      std::vector<int> freebits;  // words 1..
+      long long kmin = LLONG_MAX, kmax = LLONG_MIN;
+      while (next < tabs.size() && ntab < reserve) {
+        const DimTablePtr& T = tabs[next];
+        const int pb = T->desc.entry_bits - 1;
+        const long long tmin = T->desc.key_min, tmax = (long long)T->desc.key_min + T->desc.span - 1;
+        const long long nmin = std::min(kmin, tmin), nmax = std::max(kmax, tmax);
+        if ((nmax - nmin + 1) * 32ll > (1ll << 30)) break;
+        MergePlan::Place pl;
+        pl.group = g;
+        pl.present_bit = ntab;
+        int word = -1;
+        if (pb > 0) {
+          if (low0 - reserve >= pb) {
+            word = 0;
+          } else {
+            for (size_t z = 0; z < freebits.size() && word < 0; z++)
+              if (freebits[z] >= pb) word = (int)z + 1;
+            if (word < 0 && freebits.size() < 7) {
+              freebits.push_back(32);
+              word = (int)freebits.size();
+            }
+            if (word < 0) break;
+          }
+          pl.pay_word = word;
+          if (word == 0) {
+            pl.pay_bit = low0 - pb;
+            low0 -= pb;
+          } else {
+            pl.pay_bit = 32 - freebits[word - 1];
+            freebits[word - 1] -= pb;
+          }
+        }
+        ntab++;
+        next++;
+        kmin = nmin;
+        kmax = nmax;
+        mp->members[g].push_back({T, pl});
+        mp->place[{col, T.get()}] = pl;
+      }
+      if (ntab == 0) {  // the next table alone does not fit: leave it unplaced
+        mp->groups.pop_back();
+        mp->members.pop_back();
+        next++;
+        continue;
+      }
+      ProbeGroup& G = mp->groups[g];
+      G.key_min = (int32_t)kmin;
+      G.span = (uint32_t)(kmax - kmin + 1);
+      int words = 1;
+      while (words < 1 + (int)freebits.size()) words *= 2;
+      G.words = words;
+    }
+  }
+  // Groups beyond the per-row word or table-slot budget are left out (their
+  // tables unplaced); the others get their words and table slots in order
+  // (slot = group's first slot + present bit).
+  int off = 0, slots = 0;
+  mp->gtab0.assign(mp->groups.size() + 1, 0);
+  for (size_t g = 0; g < mp->groups.size(); g++) {
+    mp->gtab0[g] = slots;
+    if (off + mp->groups[g].words > kMaxMergedWords || slots + (int)mp->members[g].size() > kMaxMergedTables) {
+      for (auto& m : mp->members[g]) mp->place.erase({mp->groups[g].col, m.first.get()});
+      mp->members[g].clear();
+      mp->groups[g].words = 0;
+      continue;
+    }
+    mp->groups[g].word_off = off;
+    for (auto& m : mp->members[g]) {
+      m.second.slot = slots + m.second.present_bit;
+      mp->place[{mp->groups[g].col, m.first.get()}].slot = m.second.slot;
+    }
+    slots += (int)mp->members[g].size();
+    off += mp->groups[g].words;
+  }
+  mp->gtab0[mp->groups.size()] = slots;
+  mp->nmwords = off;
+}
+
+// The merged table of group g, from the cache or built now.
+svm_status merged_table(Ctx* x, MergePlan* mp, int g) {
+  ProbeGroup& G = mp->groups[g];
+  std::string key = std::to_string(G.key_min) + ":" + std::to_string(G.span) + ":" + std::to_string(G.words);
+  for (auto& m : mp->members[g])
+    key += "|" + std::to_string((uintptr_t)m.first.get()) + "@" + std::to_string(m.second.present_bit) + "." +
+           std::to_string(m.second.pay_word) + "." + std::to_string(m.second.pay_bit);
+  auto it = x->merged_cache.find(key);
+  if (it == x->merged_cache.end()) {
+    if (x->merged_cache.size() >= 64) {  // evict the least recently used
+      auto old = x->merged_cache.begin();
+      for (auto c = x->merged_cache.begin(); c != x->merged_cache.end(); ++c)
+        if (c->second.stamp < old->second.stamp) old = c;
+      x->merged_cache.erase(old);
+    }
+    MergedTable mt;
+    svm_status st = x->alloc((size_t)G.span * G.words * 4, &mt.buf);
+    if (st) return st;
+    for (size_t b0 = 0; b0 < mp->members[g].size(); b0 += kMaxMergeSrcs) {
+      // More members than one build holds: OR further builds in (all start from zero).
+      MergeBuild mb{};
+      mb.key_min = G.key_min;
+      mb.span = G.span;
+      mb.words = G.words;
+      for (size_t i = b0; i < mp->members[g].size() && mb.nsrc < kMaxMergeSrcs; i++) {
+        const auto& m = mp->members[g][i];
+        const DimDesc& d = m.first->desc;
+        mb.src[mb.nsrc++] =
+            MergeSrc{d.words, d.key_min, d.span, d.entry_bits, m.second.present_bit, m.second.pay_word, m.second.pay_bit};
+        mt.srcs.push_back(m.first);
+      }
+      if (b0 > 0) return x->fail(SVM_E_UNSUPPORTED, "more than 32 tables in one merged probe group");
+      cudaError_t e = launch_merge_build(mb, (uint32_t*)mt.buf->p, x->stream);
+      if (e) return x->cuda_fail(e, "merged table build");
+    }
+    it = x->merged_cache.emplace(key, std::move(mt)).first;
+  }
+  it->second.stamp = ++x->merged_stamp;
+  G.table = (const uint32_t*)it->second.buf->p;
+  return SVM_OK;
+}
+
+// One batched launch over queries that share a fact table: queries whose
+// probes all hit merged tables run in the merged kernel, the others in the
+// per-query batch kernel; one finalize covers both.
 svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
   const int nq = (int)items.size();
   // Union of the fact columns, identified by their storage.
@@ -880,8 +1050,6 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
     return (int)ucols.size() - 1;
   };
   std::vector<BatchQuery> qs(nq);
-  unsigned long long slot_words = 0, total_groups = 0;
-  long long lo = LLONG_MAX, hi = LLONG_MIN;
   for (int i = 0; i < nq; i++) {
     StarPlan& pl = items[i].plan;
     StarParams& P = pl.P;
@@ -914,57 +1082,186 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
       Q.xb[m] = fix(P.metrics[m].xb);
     }
     Q.ngroups = P.ngroups;
-    Q.slot_off = slot_words;
-    Q.group_off = total_groups;
-    slot_words += (unsigned long long)(P.nmetrics + 1) * P.ngroups;
-    total_groups += P.ngroups;
-    lo = std::min(lo, Q.row_begin);
-    hi = std::max(hi, Q.row_end);
   }
   if ((int)ucols.size() > kMaxBatchCols) return x->fail(SVM_E_UNSUPPORTED, "batch reads more than 12 fact columns");
-  if (hi < lo) hi = lo;
-  // Device buffers: the query table, group slots, the tile counter, finalize scratch.
-  x->scratch_reset();
-  const size_t qbytes = sizeof(BatchQuery) * nq;
-  const size_t fin_words = (total_groups + 1) / 2 + 1 + total_groups + 1 + scan_tmp_words(total_groups);
-  const size_t need = qbytes + 8 * slot_words + 8 + 8 * fin_words + 8 * 1024;
-  svm_status st = x->scratch_reserve(need);
-  if (st) return st;
-  void *dq, *slots, *ctr, *fin;
-  if ((st = x->scratch_take(qbytes, &dq)) || (st = x->scratch_take(8 * slot_words, &slots)) ||
-      (st = x->scratch_take(8, &ctr)) || (st = x->scratch_take(8 * fin_words, &fin)))
-    return st;
-  cudaError_t e = cudaMemcpyAsync(dq, qs.data(), qbytes, cudaMemcpyHostToDevice, x->stream);
-  if (!e) e = cudaMemsetAsync(slots, 0, 8 * slot_words, x->stream);
-  if (!e) e = cudaMemsetAsync(ctr, 0, 8, x->stream);
-  if (e) return x->cuda_fail(e, "batch setup");
-  BatchParams B{};
-  B.ncols = (int)ucols.size();
-  for (size_t c = 0; c < ucols.size(); c++) B.cols[c] = (const int32_t*)ucols[c];
-  B.row_begin = lo;
-  B.row_end = hi;
-  B.queries = (const BatchQuery*)dq;
-  B.nqueries = nq;
-  B.slots = (unsigned long long*)slots;
-  B.tile_counter = (unsigned long long*)ctr;
-  B.error = x->d_error;
-  // Ring depth: as deep as keeps two blocks per SM.
-  B.nstages = 2;
-  for (int nst = kStages; nst >= 2; nst--) {
-    B.nstages = nst;
-    if (batch_smem_bytes(B) <= 100 * 1024) break;
+
+  // ---- merged probe groups, and the queries they cover
+  MergePlan mp;
+  plan_merge(qs, items, &mp);
+  std::vector<int> order, legacy;
+  std::vector<MQuery> mqs(nq);
+  for (int i = 0; i < nq; i++) {
+    BatchQuery& Q = qs[i];
+    struct DimPlace {
+      bool ok = false;
+      MergePlan::Place p;
+    } dp[kMaxDims];
+    bool ok = true;
+    for (int k = 0; k < Q.nsteps && ok; k++) {
+      const Step& st = Q.steps[k];
+      if (st.kind != STEP_PROBE) continue;
+      auto f = mp.place.find({st.col, items[i].plan.dim_tables[st.dim].get()});
+      if (f == mp.place.end() || mp.groups[f->second.group].words == 0) {
+        ok = false;
+        break;
+      }
+      dp[st.dim].ok = true;
+      dp[st.dim].p = f->second;
+    }
+    if (!ok) {
+      legacy.push_back(i);
+      continue;
+    }
+    order.push_back(i);
+    // The merged kernel's descriptor: probe steps become table-slot bit tests
+    // (a folded key range becomes a range step), then the range steps.
+    MQuery M{};
+    M.row_begin = Q.row_begin;
+    M.row_end = Q.row_end;
+    M.ngroups = Q.ngroups;
+    for (int k = 0; k < Q.nsteps; k++) {
+      const Step& st = Q.steps[k];
+      if (st.kind == STEP_PROBE) {
+        const MergePlan::Place& pl = dp[st.dim].p;
+        M.probe_tab[M.nprobe++] = (uint8_t)pl.slot;
+        M.tmask |= 1ull << pl.slot;
+        M.gmask |= 1u << pl.group;
+        if (st.lo == INT_MIN && st.hi == INT_MAX) continue;
+      }
+      M.range[M.nrange++] = MRange{st.col, st.lo, st.hi};
+    }
+    auto mxt = [&](const Extract& e) {
+      MExtract r{};
+      r.mask = e.mask;
+      r.base = e.base;
+      r.col = e.col;
+      if (e.dim < 0) {
+        r.src = -1;
+        r.slot = (uint8_t)e.slot;
+        return r;
+      }
+      // A payload field at bit `shift` of the entry sits at pay_bit + shift - 1
+      // of the payload word (the present bit is not carried there).
+      const MergePlan::Place& pl = dp[e.dim].p;
+      r.src = (int16_t)(mp.groups[pl.group].word_off + pl.pay_word);
+      r.shift = (uint8_t)(pl.pay_bit + (e.mask ? e.shift - 1 : 0));
+      M.gmask |= 1u << pl.group;
+      return r;
+    };
+    M.nkeys = (uint8_t)Q.nkeys;
+    for (int k = 0; k < Q.nkeys; k++) {
+      M.kx[k] = mxt(Q.kx[k]);
+      M.krange[k] = Q.krange[k];
+      M.kstride[k] = Q.kstride[k];
+    }
+    M.nmetrics = (uint8_t)Q.nmetrics;
+    for (int m = 0; m < Q.nmetrics; m++) {
+      M.mform[m] = (uint8_t)Q.mform[m];
+      M.xa[m] = mxt(Q.xa[m]);
+      if (Q.mform[m] != MF_OPND) M.xb[m] = mxt(Q.xb[m]);
+    }
+    mqs[i] = M;
   }
-  const size_t smem = batch_smem_bytes(B);
+  const int nmerged = (int)order.size();
+  order.insert(order.end(), legacy.begin(), legacy.end());
+  svm_status st;
+  if (nmerged)
+    for (size_t g = 0; g < mp.groups.size(); g++)
+      if (mp.groups[g].words && (st = merged_table(x, &mp, (int)g))) return st;
+
+  // ---- slots and group numbering in launch order
+  std::vector<BatchQuery> dqs(nq);
+  std::vector<MQuery> dmq(nmerged);
+  unsigned long long slot_words = 0, total_groups = 0;
+  long long lo[2] = {LLONG_MAX, LLONG_MAX}, hi[2] = {LLONG_MIN, LLONG_MIN};
+  for (int j = 0; j < nq; j++) {
+    BatchQuery Q = qs[order[j]];
+    Q.slot_off = slot_words;
+    Q.group_off = total_groups;
+    slot_words += (unsigned long long)(Q.nmetrics + 1) * Q.ngroups;
+    total_groups += Q.ngroups;
+    const int part = j < nmerged ? 0 : 1;
+    lo[part] = std::min(lo[part], Q.row_begin);
+    hi[part] = std::max(hi[part], Q.row_end);
+    dqs[j] = Q;
+    if (part == 0) {
+      mqs[order[j]].slot_off = Q.slot_off;
+      dmq[j] = mqs[order[j]];
+    }
+  }
+  x->scratch_reset();
+  const size_t qbytes = sizeof(BatchQuery) * nq, mbytes = sizeof(MQuery) * nmerged;
+  const size_t fin_words = (total_groups + 1) / 2 + 1 + total_groups + 1 + scan_tmp_words(total_groups);
+  const size_t need = qbytes + mbytes + 8 * slot_words + 16 + 8 * fin_words + 8 * 1024;
+  if ((st = x->scratch_reserve(need))) return st;
+  void *dq, *dm = nullptr, *slots, *ctr, *fin;
+  if ((st = x->scratch_take(qbytes, &dq)) || (nmerged && (st = x->scratch_take(mbytes, &dm))) ||
+      (st = x->scratch_take(8 * slot_words, &slots)) || (st = x->scratch_take(16, &ctr)) ||
+      (st = x->scratch_take(8 * fin_words, &fin)))
+    return st;
+  cudaError_t e = cudaMemcpyAsync(dq, dqs.data(), qbytes, cudaMemcpyHostToDevice, x->stream);
+  if (!e && nmerged) e = cudaMemcpyAsync(dm, dmq.data(), mbytes, cudaMemcpyHostToDevice, x->stream);
+  if (!e) e = cudaMemsetAsync(slots, 0, 8 * slot_words, x->stream);
+  if (!e) e = cudaMemsetAsync(ctr, 0, 16, x->stream);
+  if (e) return x->cuda_fail(e, "batch setup");
   cudaEvent_t ev;
-  x->prof_begin(SVM_K_BATCH, &ev);
-  e = launch_batch(B, batch_grid_size(B, smem), smem, x->stream);
-  x->prof_end(SVM_K_BATCH, ev);
-  if (e) return x->cuda_fail(e, "batch kernel");
+  for (int part = 0; part < 2; part++) {
+    const int q0 = part ? nmerged : 0, qn = part ? nq - nmerged : nmerged;
+    if (!qn) continue;
+    BatchParams B{};
+    B.ncols = (int)ucols.size();
+    for (size_t c = 0; c < ucols.size(); c++) B.cols[c] = (const int32_t*)ucols[c];
+    B.row_begin = lo[part];
+    B.row_end = std::max(hi[part], lo[part]);
+    B.queries = (const BatchQuery*)dq + q0;
+    B.nqueries = qn;
+    B.slots = (unsigned long long*)slots;
+    B.tile_counter = (unsigned long long*)ctr + part;
+    B.error = x->d_error;
+    if (part == 0) {
+      B.nprobe = (int)mp.groups.size();
+      for (size_t g = 0; g < mp.groups.size(); g++) B.probe[g] = mp.groups[g];
+      B.nmwords = mp.nmwords;
+      B.mq = (const MQuery*)dm;
+      for (size_t g = 0; g < mp.gtab0.size(); g++) B.gtab0[g] = mp.gtab0[g];
+      B.nstages = 2;
+      for (int nst = kStages; nst >= 2; nst--) {
+        B.nstages = nst;
+        if (mbatch_smem_bytes(B) <= 200 * 1024) break;
+      }
+      const size_t smem = mbatch_smem_bytes(B);
+      const int grid = mbatch_grid_size(B, smem);
+      if (grid <= 0) {
+        int regs = 0, maxt = 0;
+        size_t ss = 0;
+        mbatch_attributes(&regs, &maxt, &ss);
+        return x->fail(SVM_E_UNSUPPORTED, "merged batch kernel does not fit an SM: " + std::to_string(smem) +
+                                              " B dynamic + " + std::to_string(ss) + " B static shared memory, " +
+                                              std::to_string(regs) + " registers, max " + std::to_string(maxt) +
+                                              " threads per block");
+      }
+      x->prof_begin(SVM_K_BATCH, &ev);
+      e = launch_mbatch(B, grid, smem, x->stream);
+      x->prof_end(SVM_K_BATCH, ev);
+    } else {
+      B.nstages = 2;
+      for (int nst = kStages; nst >= 2; nst--) {
+        B.nstages = nst;
+        if (batch_smem_bytes(B) <= 100 * 1024) break;
+      }
+      const size_t smem = batch_smem_bytes(B);
+      x->prof_begin(SVM_K_BATCH, &ev);
+      e = launch_batch(B, batch_grid_size(B, smem), smem, x->stream);
+      x->prof_end(SVM_K_BATCH, ev);
+    }
+    if (e) return x->cuda_fail(e, "batch kernel");
+  }
+  const BatchQuery* dQ = (const BatchQuery*)dq;
   uint32_t* flags = (uint32_t*)fin;
   unsigned long long* pos = (unsigned long long*)fin + (total_groups + 1) / 2 + 1;
   unsigned long long* scant = pos + total_groups + 1;
   x->prof_begin(SVM_K_FINALIZE, &ev);
-  e = launch_batch_finalize(B.queries, nq, B.slots, total_groups, flags, pos, scant, nullptr, x->stream);
+  e = launch_batch_finalize(dQ, nq, (unsigned long long*)slots, total_groups, flags, pos, scant, nullptr, x->stream);
   x->prof_end(SVM_K_FINALIZE, ev);
   std::vector<unsigned long long> hpos(total_groups + 1);
   if (!e) e = cudaMemcpyAsync(hpos.data(), pos, 8 * (total_groups + 1), cudaMemcpyDeviceToHost, x->stream);
@@ -979,17 +1276,18 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
   for (int k = 0; k < kMaxKeys; k++) o.key[k] = (int32_t*)all->col(k);
   for (int m = 0; m < kMaxMetrics; m++) o.sum[m] = (long long*)all->col(kMaxKeys + m);
   x->prof_begin(SVM_K_FINALIZE, &ev);
-  e = launch_batch_finalize(B.queries, nq, B.slots, total_groups, flags, pos, scant, &o, x->stream);
+  e = launch_batch_finalize(dQ, nq, (unsigned long long*)slots, total_groups, flags, pos, scant, &o, x->stream);
   x->prof_end(SVM_K_FINALIZE, ev);
   if (e) return x->cuda_fail(e, "batch write");
   if ((st = sync_and_check(x, "batch write"))) return st;
-  for (int i = 0; i < nq; i++) {
-    const BatchQuery& Q = qs[i];
+  for (int j = 0; j < nq; j++) {
+    const BatchQuery& Q = dqs[j];
+    const BatchItem& it = items[order[j]];
     auto out = std::make_shared<Object>();
-    out->id = items[i].id;
+    out->id = it.id;
     out->version = x->next_version++;
     out->ncols = Q.nkeys + Q.nmetrics;
-    out->types = items[i].plan.out_types;
+    out->types = it.plan.out_types;
     for (int k = 0; k < Q.nkeys; k++) out->storage.push_back(all->storage[k]);
     for (int m = 0; m < Q.nmetrics; m++) out->storage.push_back(all->storage[kMaxKeys + m]);
     out->row0 = hpos[Q.group_off];
@@ -997,7 +1295,7 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
     out->has_bulks = true;
     out->bulk0_rows = out->nrows;
     out->source_rows = out->nrows;
-    x->objects[items[i].id] = out;
+    x->objects[it.id] = out;
   }
   return SVM_OK;
 }

@@ -81,7 +81,7 @@ __host__ __device__ inline uint32_t mix32(uint32_t x) {
 }
 
 // ---------------------------------------------------------------- fused star query
-enum StepKind : int { STEP_RANGE = 0, STEP_PROBE = 1 };
+enum StepKind : int { STEP_RANGE = 0, STEP_PROBE = 1, STEP_MPROBE = 2 };
 
 struct Step {
   int kind;
@@ -99,6 +99,9 @@ struct Step {
   // 1: evaluate the next step in the same pass (its lookups in flight with
   // this step's), set by the planner for consecutive global-table probes.
   int fuse_next;
+  // STEP_MPROBE (merged batch): the table's entry sits at bit `mbit` of merged
+  // probe word `mword`; `col` < 0 when no key range is folded in.
+  int mword, mbit;
 };
 
 // A value the aggregation reads: a staged fact column, or a payload field of a
@@ -168,6 +171,74 @@ struct StarParams {
 // range covers a tile runs its own steps and aggregation on the staged tile.
 constexpr int kMaxBatchCols = 12;
 
+// Merged probe tables (batch mode).  The dense tables that a batch's queries
+// probe with the same fact column are concatenated entry by entry: for key k
+// the merged table holds `words` 32-bit words; word 0 starts with the present
+// bits of the group's tables (table i of the group at bit i), and each table's
+// payload bits sit at a fixed word and bit after them.  One lookup per row and
+// group then serves every query of the batch that probes any of those tables.
+constexpr int kMaxProbeGroups = 8;
+constexpr int kMaxMergedWords = 16;   // merged words per row over all groups
+constexpr int kMBatchWarps = 16;      // consumer warps of the merged batch kernel
+
+struct ProbeGroup {
+  int col;                  // union fact column slot of the key
+  int words;                // 1, 2, 4 or 8 words per key
+  int32_t key_min;
+  uint32_t span;
+  int word_off;             // first merged word of the group in the per-row layout
+  const uint32_t* table;    // span * words
+};
+
+struct MergeSrc {           // one dense table placed into a merged table
+  const uint32_t* words;
+  int32_t key_min;
+  uint32_t span;
+  int entry_bits;
+  int present_bit;          // in word 0
+  int pay_word, pay_bit;    // the entry's payload (entry >> 1, entry_bits - 1 bits)
+};
+
+constexpr int kMaxMergeSrcs = 32;
+struct MergeBuild {
+  int32_t key_min;
+  uint32_t span;
+  int words;
+  int nsrc;
+  MergeSrc src[kMaxMergeSrcs];
+};
+
+// The merged kernel's own compact query descriptor (prefetched per warp).
+// Probe steps are bit tests against per-tile row bitmaps of the merged tables'
+// present bits (table slots 0..63); range steps test staged fact values.
+constexpr int kMaxMergedTables = 64;
+
+struct MExtract {
+  int16_t src;          // -1: fact column `slot`; else merged word index
+  uint8_t slot, shift;
+  uint32_t mask;
+  int32_t base;
+  int32_t pad;
+  const int32_t* col;   // non-null: value = col[field] + base
+};
+
+struct MRange {
+  int32_t col, lo, hi;
+};
+
+struct MQuery {
+  long long row_begin, row_end;
+  unsigned long long slot_off, ngroups;
+  unsigned long long tmask;         // table slots the query tests
+  uint32_t gmask;                   // probe groups whose words it reads
+  uint8_t nprobe, nrange, nkeys, nmetrics;
+  uint8_t probe_tab[kMaxSteps];
+  uint8_t mform[4];
+  uint32_t krange[kMaxKeys], kstride[kMaxKeys];
+  MRange range[kMaxSteps];
+  MExtract kx[kMaxKeys], xa[kMaxMetrics], xb[kMaxMetrics];
+};
+
 struct BatchQuery {                 // in device memory, one per query
   long long row_begin, row_end;     // base rows this query reads
   int nsteps;
@@ -183,6 +254,7 @@ struct BatchQuery {                 // in device memory, one per query
   unsigned long long ngroups;
   unsigned long long slot_off;      // sums at slots + slot_off, counts after nmetrics * ngroups
   unsigned long long group_off;     // this query's first group in the batch's group numbering
+  uint32_t gmask;                   // merged probe groups the query reads
 };
 
 struct BatchParams {
@@ -195,6 +267,11 @@ struct BatchParams {
   unsigned long long* slots;
   unsigned long long* tile_counter; // zeroed before the launch
   int* error;
+  int nprobe;                       // merged batch kernel: probe groups
+  ProbeGroup probe[kMaxProbeGroups];
+  int nmwords;                      // merged words per row
+  const MQuery* mq;                 // merged kernel: descriptors (nqueries)
+  int gtab0[kMaxProbeGroups + 1];   // group g's tables are slots [gtab0[g], gtab0[g + 1]), in present-bit order
 };
 
 // Fills the flattened copies (Step table fields, Extract descriptors) from the

@@ -36,10 +36,13 @@ def test_batch_equals_one_launch_per_query(engine_factory, mode):
     eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, join_mode=mode)
     W.load_batch(eng, bw)
     one = singles(eng, bw)
+    first = batched(eng, bw)  # builds and caches the merged probe tables
     n0 = eng.kernel_launches()
     many = batched(eng, bw)
     launches = eng.kernel_launches() - n0
     assert launches < 10, launches  # one scan kernel plus the finalize kernels
+    for i in one:
+        np.testing.assert_array_equal(first[i][1], many[i][1])
     nonempty = 0
     for i in one:
         np.testing.assert_array_equal(many[i][0], one[i][0], err_msg=f"keys of query {i}")
@@ -77,6 +80,13 @@ def test_batch_mixed_with_selects_and_unbatchable(engine_factory):
         fact_pipeline("x_scalar", "lo_q3", schema, [], [], "", "$(0.7)+$(0.8)",
                       predication="$(0.2)==4"),
     ]
+    # Sparse keys give a hash-layout table: that query takes the per-query
+    # batch kernel beside the merged one.
+    sk = np.arange(0, bw.fact.n_part, 97, dtype=np.int32)
+    eng.put("sparse", [sk, (sk % 13).astype(np.int32)])
+    bw.dim_pipelines.append(dim_pipeline("b_sparse", "sparse", W.int_schema(2), "$(0.0),$(0.1)", None))
+    extra.append(fact_pipeline("x_hash", "lo_q4", schema, ["b_sparse"], [("$(0.4)", "$(1.0)")], "$(1.1)",
+                               "$(0.7)-$(0.8)"))
     eng.view("lo_none", "lineorder", 10, 0)
     extra.append(fact_pipeline("x_none", "lo_none", schema, ["b_date"], [("$(0.0)", "$(1.0)")], "$(1.1)",
                                "$(0.7)"))
