@@ -1,18 +1,19 @@
 // Batched star queries with merged probe tables.
 //
 // One persistent block per SM scans the union of a batch's fact columns once
-// (bulk-copy ring, dynamic tile hand-out).  For every 1024-row tile the block
-// first looks every row up once in each merged probe table the tile's queries
-// need (ProbeGroup: the dense dimension tables probed through one fact column,
-// concatenated per key), keeps the merged words in shared memory and turns
-// each needed table's present bits into a 1024-bit row bitmap with warp
-// ballots.  Then its warps take the tile's queries one at a time (the next
-// query's descriptor is copied in while one runs).  A query's probe steps are
-// one AND of a bitmap word per lane; its range steps test staged fact values,
-// with ballots over every row while many rows live, else only the live rows;
-// only its surviving rows reach the int64 group slots.  The lookups are thus
-// shared by every query of the batch, and a query's work per tile is a few
-// instructions per 32 rows.
+// (bulk-copy ring, dynamic tile hand-out).  The producer warp runs one tile
+// ahead of the consumers: once a tile has landed it looks every row up in
+// each merged probe table the tile's queries need (ProbeGroup: the dense
+// dimension tables probed through one fact column, concatenated per key) with
+// asynchronous gathers into one of two merged-word buffers, whose completion
+// an mbarrier tracks.  The consumer warps turn each needed table's present
+// bits into a 1024-bit row bitmap (a 32 x 32 bit transpose per 32 rows), then
+// take the tile's queries one at a time (the next query's descriptor is
+// copied in while one runs).  A query's probe steps are one AND of a bitmap
+// word per lane; its range steps test staged fact values, with ballots over
+// every row while many rows live, else only the live rows; only its surviving
+// rows reach the int64 group slots.  The lookups are thus shared by every
+// query of the batch and overlap the previous tile's query work.
 #include <climits>
 
 #include "kern_common.cuh"
@@ -21,8 +22,10 @@
 namespace svm {
 namespace {
 
-constexpr int kMBThreads = (kMBatchWarps + 1) * 32;
+constexpr int kFillWarps = 4;  // warp kMBatchWarps also issues the bulk copies
+constexpr int kMBThreads = (kMBatchWarps + kFillWarps) * 32;
 constexpr int kMBConsumers = kMBatchWarps * 32;
+constexpr int kFillRows = kTileRows / kFillWarps;
 constexpr uint32_t kPolls = 1u << 22;
 
 __device__ __forceinline__ void consumer_bar() {
@@ -51,41 +54,75 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 // A value for the aggregation: a staged fact value, or a payload field of a
-// merged probe word (optionally a row index into `col`), plus `base`.
+// merged probe word (optionally a row index into `col`), plus `base`.  A
+// group's merged words sit row-major: word w of row r at
+// group_first_word * kTileRows + r * words + w.
 __device__ __forceinline__ uint32_t mx(const MExtract& x, const int32_t* stage, const uint32_t* mw, int row) {
   if (x.src < 0) return (uint32_t)stage[x.slot * kTileRows + row] + (uint32_t)x.base;
-  uint32_t v = (mw[x.src * kTileRows + row] >> x.shift) & x.mask;
+  uint32_t v = (mw[x.src * kTileRows + row * x.stride + x.slot] >> x.shift) & x.mask;
   if (x.col) v = (uint32_t)__ldg(x.col + v);
   return v + (uint32_t)x.base;
 }
 
-// Looks one 32-row chunk up in a merged table (lane = row of the chunk), keeps
-// the row's merged words and returns word 0 (the present bits).
-template <int W>
-__device__ __forceinline__ uint32_t fill_row(const ProbeGroup& G, const int32_t* stage, uint32_t* mw, int row) {
+// Asynchronous gather of 4, 8 or 16 bytes; with `valid` false it writes zeros
+// and reads nothing.
+// The merged tables are gathered with an L2 evict-last policy, the fact
+// stream with evict-first, so the scan does not push the tables out of L2.
+template <int kBytes>
+__device__ __forceinline__ void cp_async_zfill(void* dst, const void* src, bool valid, uint64_t policy) {
+  if (kBytes == 16)
+    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2, %3;" ::"r"(smem_u32(dst)), "l"(src),
+                 "r"(valid ? 16 : 0), "l"(policy)
+                 : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], %2, %3, %4;" ::"r"(smem_u32(dst)), "l"(src),
+                 "n"(kBytes), "r"(valid ? kBytes : 0), "l"(policy)
+                 : "memory");
+}
+
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+__device__ __forceinline__ void bulk_g2s_hint(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                              uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+
+// Starts the lookup of one row in a merged table: the entry's words are
+// copied to the row's slot of the group's region (zeros when the key is
+// outside the table).
+__device__ __forceinline__ void fill_issue(const ProbeGroup& G, const int32_t* stage, uint32_t* mwb, int row,
+                                           uint64_t pol) {
   const uint32_t off = (uint32_t)stage[G.col * kTileRows + row] - (uint32_t)G.key_min;
   const bool in = off < G.span;
+  const int W = G.words;
   const uint32_t* src = G.table + (size_t)(in ? off : 0u) * W;
-  uint32_t v[W];
+  uint32_t* dst = mwb + G.word_off * kTileRows + row * W;
   if (W == 1) {
-    v[0] = in ? __ldg(src) : 0u;
+    cp_async_zfill<4>(dst, src, in, pol);
   } else if (W == 2) {
-    const uint2 a = in ? __ldg(reinterpret_cast<const uint2*>(src)) : make_uint2(0u, 0u);
-    v[0] = a.x;
-    v[1 % W] = a.y;
+    cp_async_zfill<8>(dst, src, in, pol);
   } else {
-#pragma unroll
-    for (int h = 0; h < W / 4; h++) {
-      const uint4 a = in ? __ldg(reinterpret_cast<const uint4*>(src) + h) : make_uint4(0u, 0u, 0u, 0u);
-      v[(4 * h + 0) % W] = a.x;
-      v[(4 * h + 1) % W] = a.y;
-      v[(4 * h + 2) % W] = a.z;
-      v[(4 * h + 3) % W] = a.w;
-    }
+    for (int h = 0; h < W; h += 4) cp_async_zfill<16>(dst + h, src + h, in, pol);
   }
-#pragma unroll
-  for (int w = 0; w < W; w++) mw[(G.word_off + w) * kTileRows + row] = v[w];
-  return v[0];
+}
+
+// Each lane's completed gathers count one arrival on `bar`.
+__device__ __forceinline__ void cp_async_arrive(uint64_t* bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // 32 x 32 bit transpose across a warp: lane i holds row i on entry (bit j =
@@ -203,17 +240,40 @@ __device__ __forceinline__ void copy_desc(MQuery* dst, const MQuery* src, int la
   cp_async_commit();
 }
 
+// The queries active on the tile starting at `tile_start` and the probe
+// groups they need (every lane of the calling warp gets `need`; with `list`
+// the active query indices are written to act[0, na)).
+__device__ __forceinline__ uint32_t tile_queries(const long long* qlo, const long long* qhi, const uint32_t* qg,
+                                                 int nq, long long tile_start, uint16_t* act, bool list, int lane,
+                                                 uint32_t lt, int* na_out) {
+  const long long tile_end = tile_start + kTileRows;
+  uint32_t need = 0;
+  int na = 0;
+  for (int base = 0; base < nq; base += 32) {
+    const int q = base + lane;
+    const bool a = q < nq && qlo[q] < tile_end && qhi[q] > tile_start;
+    if (a) need |= qg[q];
+    const uint32_t bq = __ballot_sync(0xffffffffu, a);
+    if (list && a) act[na + __popc(bq & lt)] = (uint16_t)q;
+    na += __popc(bq);
+  }
+  *na_out = na;
+  return __reduce_or_sync(0xffffffffu, need);
+}
+
 __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_constant__ BatchParams B) {
   extern __shared__ __align__(128) uint8_t dyn[];
   __shared__ uint64_t full[kStages], empty[kStages];
+  __shared__ uint64_t fill_full[2], fill_empty[2];
   __shared__ long long stage_tile[kStages];
   __shared__ long long s_tile;
   __shared__ int s_next;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ncols = B.ncols, nst = B.nstages, nq = B.nqueries;
+  const size_t mw_words = (size_t)B.nmwords * kTileRows;
   int32_t* ring = reinterpret_cast<int32_t*>(dyn);
-  uint32_t* mw = reinterpret_cast<uint32_t*>(dyn + (size_t)nst * ncols * kTileRows * 4);
-  uint32_t* bm = mw + (size_t)B.nmwords * kTileRows;
+  uint32_t* mwbuf = reinterpret_cast<uint32_t*>(dyn + (size_t)nst * ncols * kTileRows * 4);  // two buffers
+  uint32_t* bm = mwbuf + 2 * mw_words;
   MQuery* dbuf = reinterpret_cast<MQuery*>(bm + kMaxMergedTables * kBmStride);
   long long* qlo = reinterpret_cast<long long*>(dbuf + 2 * kMBatchWarps);
   long long* qhi = qlo + nq;
@@ -223,6 +283,10 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
     for (int s = 0; s < nst; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&fill_full[b], 32 * kFillWarps);  // one arrival per fill lane
+      mbar_init(&fill_empty[b], 1);
     }
     mbar_fence_init();
   }
@@ -235,48 +299,83 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
   const long long a0 = B.row_begin & ~3ll;
   const long long end4 = (B.row_end + 3) & ~3ll;
   const long long ntiles = (B.row_end - a0 + kTileRows - 1) / kTileRows;
+  const uint32_t lt = lane_lt();
 
-  if (warp == kMBatchWarps) {
-    // Producer: one thread hands out tiles and issues their bulk copies.
-    if (lane == 0) {
-      long long issued = 0;
-      for (;; issued++) {
-        const int s = (int)(issued % nst);
-        const long long k = issued / nst;
-        if (k > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)((k - 1) & 1), kPolls)) {
-          raise_error(B.error, DERR_TIMEOUT);
-          break;
-        }
-        const long long t = (long long)atomicAdd(B.tile_counter, 1ull);
-        if (t >= ntiles) {
-          stage_tile[s] = -1;  // end of the scan
-          mbar_arrive(&full[s]);
-          issued++;
-          break;
-        }
-        stage_tile[s] = t;
-        const long long start = a0 + t * kTileRows;
-        const long long stop = start + kTileRows < end4 ? start + kTileRows : end4;
-        const uint32_t bytes = (uint32_t)((stop - start) * 4);
-        mbar_arrive_expect_tx(&full[s], bytes * (uint32_t)ncols);
-        for (int c = 0; c < ncols; c++)
-          bulk_g2s(ring + ((size_t)s * ncols + c) * kTileRows, B.cols[c] + start, bytes, &full[s]);
+  if (warp >= kMBatchWarps) {
+    // Fill warps.  Lane 0 of the first claims tiles and issues their bulk
+    // copies; each fill warp issues the lookups of its quarter of a tile's
+    // rows once the tile has landed.
+    const int fw = warp - kMBatchWarps;
+    const bool tma = fw == 0;
+    const uint64_t pol_tab = policy_evict_last(), pol_fact = policy_evict_first();
+    long long last_real = -1, last_seen = -1;  // lane 0: last tile copied / last tile waited for
+    auto issue_tile = [&](long long i) -> bool {  // lane 0 only; false on a timeout
+      const int s = (int)(i % nst);
+      if (i >= nst && !mbar_wait_bounded(&empty[s], (uint32_t)((i / nst - 1) & 1), kPolls)) return false;
+      const long long t = (long long)atomicAdd(B.tile_counter, 1ull);
+      if (t >= ntiles) {
+        stage_tile[s] = -1;  // end of the scan
+        mbar_arrive(&full[s]);
+        return true;
       }
-      // Every copy issued lands before the block may exit.
-      const long long first = issued > nst ? issued - nst : 0;
-      for (long long q = first; q < issued; q++)
-        mbar_wait_bounded(&full[q % nst], (uint32_t)((q / nst) & 1), kPolls);
+      stage_tile[s] = t;
+      const long long start = a0 + t * kTileRows;
+      const long long stop = start + kTileRows < end4 ? start + kTileRows : end4;
+      const uint32_t bytes = (uint32_t)((stop - start) * 4);
+      mbar_arrive_expect_tx(&full[s], bytes * (uint32_t)ncols);
+      for (int c = 0; c < ncols; c++)
+        bulk_g2s_hint(ring + ((size_t)s * ncols + c) * kTileRows, B.cols[c] + start, bytes, &full[s], pol_fact);
+      last_real = i;
+      return true;
+    };
+    int ok = 1;
+    if (tma && lane == 0) ok = issue_tile(0);
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    for (long long i = 0; ok; i++) {
+      const int s = (int)(i % nst), b = (int)(i & 1);
+      bool good = mbar_wait_bounded(&full[s], (uint32_t)((i / nst) & 1), kPolls);
+      if (good && i >= 2) good = mbar_wait_bounded(&fill_empty[b], (uint32_t)((i / 2 - 1) & 1), kPolls);
+      if (!__all_sync(0xffffffffu, good)) {
+        if (lane == 0) raise_error(B.error, DERR_TIMEOUT);
+        break;
+      }
+      last_seen = i;
+      const long long t = stage_tile[s];
+      if (t < 0) {
+        mbar_arrive(&fill_full[b]);  // every fill lane: lets the consumers reach the end marker
+        break;
+      }
+      int na;
+      const uint32_t need = tile_queries(qlo, qhi, qg, nq, a0 + t * kTileRows, nullptr, false, lane, lt, &na);
+      const int32_t* stage = ring + (size_t)s * ncols * kTileRows;
+      uint32_t* mwb = mwbuf + (size_t)b * mw_words;
+      for (uint32_t mm = need; mm; mm &= mm - 1) {
+        const ProbeGroup& G = B.probe[__ffs(mm) - 1];
+        for (int row = fw * kFillRows + lane; row < (fw + 1) * kFillRows; row += 32)
+          fill_issue(G, stage, mwb, row, pol_tab);
+      }
+      cp_async_arrive(&fill_full[b]);
+      if (tma) {
+        if (lane == 0) ok = issue_tile(i + 1);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok && lane == 0) raise_error(B.error, DERR_TIMEOUT);
+      }
     }
+    // Every copy issued lands before the block may exit (a tile issued but
+    // never waited for exists only after a timeout).
+    if (tma && lane == 0 && last_real > last_seen)
+      mbar_wait_bounded(&full[last_real % nst], (uint32_t)((last_real / nst) & 1), kPolls);
+    cp_async_wait<0>();
     return;
   }
 
-  const uint32_t lt = lane_lt();
   MQuery* mybuf = dbuf + 2 * warp;
   for (long long i = 0;; i++) {
-    const int s = (int)(i % nst);
-    const uint32_t parity = (uint32_t)((i / nst) & 1);
+    const int s = (int)(i % nst), b = (int)(i & 1);
+    const uint32_t sp = (uint32_t)((i / nst) & 1), bp = (uint32_t)((i / 2) & 1);
     if (tid == 0) {
-      s_tile = mbar_wait_bounded(&full[s], parity, kPolls) ? stage_tile[s] : -2;
+      const bool good = mbar_wait_bounded(&fill_full[b], bp, kPolls) && mbar_wait_bounded(&full[s], sp, kPolls);
+      s_tile = good ? stage_tile[s] : -2;
       s_next = 0;
     }
     consumer_bar();
@@ -285,23 +384,17 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
       if (t == -2 && tid == 0) raise_error(B.error, DERR_TIMEOUT);
       break;
     }
-    if (tid != 0) mbar_wait_bounded(&full[s], parity, kPolls);  // completes at once: acquires the copies
-    const int32_t* stage = ring + (size_t)s * ncols * kTileRows;
-    const long long tile_start = a0 + t * kTileRows, tile_end = tile_start + kTileRows;
-    // The tile's queries (warp 0 lists them) and the probe groups they need.
-    uint32_t need = 0;
-    int na = 0;
-    for (int base = 0; base < nq; base += 32) {
-      const int q = base + lane;
-      const bool a = q < nq && qlo[q] < tile_end && qhi[q] > tile_start;
-      if (a) need |= qg[q];
-      const uint32_t bq = __ballot_sync(0xffffffffu, a);
-      if (warp == 0 && a) act[na + __popc(bq & lt)] = (uint16_t)q;
-      na += __popc(bq);
+    if (tid != 0) {  // both phases are complete: these acquire the copies at once
+      mbar_wait_bounded(&full[s], sp, kPolls);
+      mbar_wait_bounded(&fill_full[b], bp, kPolls);
     }
-    need = __reduce_or_sync(0xffffffffu, need);
-    // Merged words of every row; the present bits, transposed, give each
-    // table's row bitmap.
+    const int32_t* stage = ring + (size_t)s * ncols * kTileRows;
+    const uint32_t* mw = mwbuf + (size_t)b * mw_words;
+    const long long tile_start = a0 + t * kTileRows, tile_end = tile_start + kTileRows;
+    int na;
+    const uint32_t need = tile_queries(qlo, qhi, qg, nq, tile_start, act, warp == 0, lane, lt, &na);
+    // Each needed table's present bits as a row bitmap: word 0 of each row's
+    // entry, transposed per 32 rows.
     const int ng = __popc(need);
     for (int it = warp; it < ng * kChunks; it += kMBatchWarps) {
       const int gsel = it / kChunks, chunk = it % kChunks;
@@ -309,21 +402,14 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
       for (int z = 0; z < gsel; z++) mm &= mm - 1;
       const int g = __ffs(mm) - 1;
       const ProbeGroup& G = B.probe[g];
-      const int row = chunk * 32 + lane;
-      uint32_t present;
-      switch (G.words) {
-        case 1: present = fill_row<1>(G, stage, mw, row); break;
-        case 2: present = fill_row<2>(G, stage, mw, row); break;
-        case 4: present = fill_row<4>(G, stage, mw, row); break;
-        default: present = fill_row<8>(G, stage, mw, row); break;
-      }
-      present = transpose32(present, lane);
+      const uint32_t present =
+          transpose32(mw[G.word_off * kTileRows + (chunk * 32 + lane) * G.words], lane);
       const int t0 = B.gtab0[g];
       if (lane < B.gtab0[g + 1] - t0) bm[(t0 + lane) * kBmStride + chunk] = present;
     }
     consumer_bar();
-    // Queries, claimed one at a time; the next one's descriptor is copied while
-    // this one runs.
+    // Queries, claimed one at a time; the next one's descriptor is copied in
+    // while this one runs.
     int k = 0;
     if (lane == 0) k = atomicAdd(&s_next, 1);
     k = __shfl_sync(0xffffffffu, k, 0);
@@ -349,7 +435,10 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
     }
     cp_async_wait<0>();
     consumer_bar();
-    if (tid == 0) mbar_arrive(&empty[s]);
+    if (tid == 0) {
+      mbar_arrive(&empty[s]);
+      mbar_arrive(&fill_empty[b]);
+    }
   }
 }
 
@@ -386,7 +475,7 @@ cudaError_t launch_merge_build(const MergeBuild& m, uint32_t* out, cudaStream_t 
 }
 
 size_t mbatch_smem_bytes(const BatchParams& b) {
-  return (size_t)b.nstages * b.ncols * kTileRows * 4 + (size_t)b.nmwords * kTileRows * 4 +
+  return (size_t)b.nstages * b.ncols * kTileRows * 4 + 2 * (size_t)b.nmwords * kTileRows * 4 +
          (size_t)kMaxMergedTables * kBmStride * 4 + sizeof(MQuery) * 2 * kMBatchWarps +
          (size_t)b.nqueries * (8 + 8 + 4 + 2) + 16;
 }
@@ -394,7 +483,7 @@ size_t mbatch_smem_bytes(const BatchParams& b) {
 int mbatch_grid_size(const BatchParams& b, size_t smem) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(mbatch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    cudaFuncSetAttribute(mbatch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024);
     attr = true;
   }
   int per_sm = 0;

@@ -1143,7 +1143,9 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
       // A payload field at bit `shift` of the entry sits at pay_bit + shift - 1
       // of the payload word (the present bit is not carried there).
       const MergePlan::Place& pl = dp[e.dim].p;
-      r.src = (int16_t)(mp.groups[pl.group].word_off + pl.pay_word);
+      r.src = (int16_t)mp.groups[pl.group].word_off;
+      r.slot = (uint8_t)pl.pay_word;
+      r.stride = mp.groups[pl.group].words;
       r.shift = (uint8_t)(pl.pay_bit + (e.mask ? e.shift - 1 : 0));
       M.gmask |= 1u << pl.group;
       return r;
@@ -1227,7 +1229,7 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
       B.nstages = 2;
       for (int nst = kStages; nst >= 2; nst--) {
         B.nstages = nst;
-        if (mbatch_smem_bytes(B) <= 200 * 1024) break;
+        if (mbatch_smem_bytes(B) <= 226 * 1024) break;
       }
       const size_t smem = mbatch_smem_bytes(B);
       const int grid = mbatch_grid_size(B, smem);

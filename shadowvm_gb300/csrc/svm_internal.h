@@ -214,11 +214,11 @@ struct MergeBuild {
 constexpr int kMaxMergedTables = 64;
 
 struct MExtract {
-  int16_t src;          // -1: fact column `slot`; else merged word index
-  uint8_t slot, shift;
+  int16_t src;          // -1: fact column `slot`; else the group's first merged word
+  uint8_t slot, shift;  // merged: `slot` = word within the group's entry
   uint32_t mask;
   int32_t base;
-  int32_t pad;
+  int32_t stride;       // merged: the group's words per row
   const int32_t* col;   // non-null: value = col[field] + base
 };
 
