@@ -8,9 +8,43 @@
 namespace svm {
 
 DevBuf::~DevBuf() {
-  if (p) {
+  if (!p) return;
+  if (ctx)
+    ctx->release(p, bytes);
+  else
     cudaFree(p);
-    if (ctx) ctx->in_use -= bytes;
+}
+
+namespace {
+constexpr size_t kPoolMaxBlock = size_t(512) << 20;  // larger blocks are freed at once
+constexpr size_t kPoolCap = size_t(4) << 30;         // pooled bytes kept at most
+
+// Size classes: four per doubling above 4 KB (at most 25% rounding).
+size_t size_class(size_t bytes) {
+  if (bytes <= 4096) return (bytes + 255) & ~size_t(255);
+  size_t p2 = 4096;
+  while (p2 * 2 < bytes) p2 *= 2;
+  const size_t q = p2 / 4;
+  return (bytes + q - 1) / q * q;
+}
+}  // namespace
+
+void Ctx::release(void* p, size_t bytes) {
+  in_use -= bytes;
+  if (bytes <= kPoolMaxBlock && pooled + bytes <= kPoolCap) {
+    pool.emplace(bytes, p);
+    pooled += bytes;
+    return;
+  }
+  cudaFree(p);
+}
+
+void Ctx::trim_pool(size_t keep) {
+  while (pooled > keep && !pool.empty()) {
+    auto it = std::prev(pool.end());  // largest first
+    cudaFree(it->second);
+    pooled -= it->first;
+    pool.erase(it);
   }
 }
 
@@ -21,11 +55,27 @@ svm_status Ctx::cuda_fail(cudaError_t e, const char* what) {
 
 svm_status Ctx::alloc(size_t bytes, DevBufPtr* out, bool zero) {
   if (bytes == 0) bytes = 256;
+  if (bytes <= kPoolMaxBlock) bytes = size_class(bytes);
   if (cfg.hbm_budget_bytes && in_use + bytes > cfg.hbm_budget_bytes)
     return fail(SVM_E_OOM_BUDGET, "HBM budget exceeded: " + std::to_string(in_use) + " + " +
                                       std::to_string(bytes) + " > " + std::to_string(cfg.hbm_budget_bytes));
   auto b = std::make_shared<DevBuf>();
-  cudaError_t e = cudaMalloc(&b->p, bytes);
+  cudaError_t e = cudaSuccess;
+  auto hit = pool.find(bytes);
+  if (hit != pool.end()) {
+    b->p = hit->second;
+    pooled -= bytes;
+    pool.erase(hit);
+  } else {
+    if (cfg.hbm_budget_bytes && in_use + pooled + bytes > cfg.hbm_budget_bytes)
+      trim_pool(cfg.hbm_budget_bytes > in_use + bytes ? cfg.hbm_budget_bytes - in_use - bytes : 0);
+    e = cudaMalloc(&b->p, bytes);
+    if (e == cudaErrorMemoryAllocation && pooled) {
+      cudaGetLastError();
+      trim_pool(0);
+      e = cudaMalloc(&b->p, bytes);
+    }
+  }
   if (e != cudaSuccess) {
     b->p = nullptr;
     cudaGetLastError();
@@ -181,6 +231,7 @@ void svm_destroy(svm_ctx* c) {
   x->merged_cache.clear();
   x->dim_cache.clear();
   x->scratch.reset();
+  x->trim_pool(0);
   for (auto e : x->event_pool) cudaEventDestroy(e);
   if (x->d_error) cudaFree(x->d_error);
   if (x->stream) cudaStreamDestroy(x->stream);

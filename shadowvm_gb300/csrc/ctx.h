@@ -89,7 +89,12 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   std::recursive_mutex mu;
   std::string err;
-  size_t in_use = 0;
+  size_t in_use = 0;                          // bytes of live allocations
+  // Freed blocks kept for reuse (all work runs on `stream`, so a block handed
+  // out again is only written after earlier work on it).  Keyed by size
+  // class; charged to the budget until trimmed.
+  std::multimap<size_t, void*> pool;
+  size_t pooled = 0;
   unsigned long long next_version = 1;
   std::map<std::string, ObjectPtr> objects;
   std::map<std::string, DimTablePtr> dim_cache;
@@ -114,6 +119,8 @@ struct Ctx {
 
   // Allocation charged to the budget (zero-filled when `zero`).
   svm_status alloc(size_t bytes, DevBufPtr* out, bool zero = false);
+  void release(void* p, size_t bytes);        // a DevBuf's block: back to the pool or freed
+  void trim_pool(size_t keep);                // frees pooled blocks until at most `keep` bytes stay
   // Scratch: reset() then take() pieces; valid until the next reset().
   void scratch_reset() { scratch_used = 0; }
   svm_status scratch_take(size_t bytes, void** out);

@@ -1,19 +1,19 @@
 // Batched star queries with merged probe tables.
 //
 // One persistent block per SM scans the union of a batch's fact columns once
-// (bulk-copy ring, dynamic tile hand-out).  The producer warp runs one tile
-// ahead of the consumers: once a tile has landed it looks every row up in
+// (bulk-copy ring, dynamic tile hand-out).  Four fill warps run one tile
+// ahead of the consumers: once a tile has landed they look every row up in
 // each merged probe table the tile's queries need (ProbeGroup: the dense
 // dimension tables probed through one fact column, concatenated per key) with
 // asynchronous gathers into one of two merged-word buffers, whose completion
 // an mbarrier tracks.  The consumer warps turn each needed table's present
 // bits into a 1024-bit row bitmap (a 32 x 32 bit transpose per 32 rows), then
-// take the tile's queries one at a time (the next query's descriptor is
-// copied in while one runs).  A query's probe steps are one AND of a bitmap
-// word per lane; its range steps test staged fact values, with ballots over
-// every row while many rows live, else only the live rows; only its surviving
-// rows reach the int64 group slots.  The lookups are thus shared by every
-// query of the batch and overlap the previous tile's query work.
+// take the tile's queries one at a time; every query's descriptor stays in
+// shared memory for the whole launch.  A query's probe steps are one AND of a
+// bitmap word per lane; its range steps test staged fact values, with ballots
+// over every row while many rows live, else only the live rows; only its
+// surviving rows reach the int64 group slots.  The lookups are thus shared by
+// every query of the batch and overlap the previous tile's query work.
 #include <climits>
 
 #include "kern_common.cuh"
@@ -40,27 +40,20 @@ __device__ __forceinline__ uint32_t lane_lt() {
 
 constexpr int kChunks = kTileRows / 32;     // bitmap words per tile
 constexpr int kBmStride = kChunks + 1;      // a table's bitmap row, padded (conflict-free stores)
-constexpr int kDescChunks = (int)(sizeof(MQuery) / 16);
+static_assert(sizeof(MQuery) == 240 && sizeof(MExtract) == 12, "descriptor layout");
 constexpr int kDenseRows = 256;             // live rows above which a range test runs on every row
-static_assert(sizeof(MQuery) % 16 == 0 && kDescChunks <= 32, "MQuery is copied in 16-byte pieces by one warp");
 
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // A value for the aggregation: a staged fact value, or a payload field of a
-// merged probe word (optionally a row index into `col`), plus `base`.  A
-// group's merged words sit row-major: word w of row r at
+// merged probe word (optionally a row index into a gather column), plus
+// `base`.  A group's merged words sit row-major: word w of row r at
 // group_first_word * kTileRows + r * words + w.
-__device__ __forceinline__ uint32_t mx(const MExtract& x, const int32_t* stage, const uint32_t* mw, int row) {
+__device__ __forceinline__ uint32_t mx(const MExtract& x, const BatchParams& B, const int32_t* stage,
+                                       const uint32_t* mw, int row) {
   if (x.src < 0) return (uint32_t)stage[x.slot * kTileRows + row] + (uint32_t)x.base;
-  uint32_t v = (mw[x.src * kTileRows + row * x.stride + x.slot] >> x.shift) & x.mask;
-  if (x.col) v = (uint32_t)__ldg(x.col + v);
+  uint32_t v = (mw[x.src * kTileRows + row * (x.sg & 15) + x.slot] >> x.shift) & x.mask;
+  if (x.sg >> 4) v = (uint32_t)__ldg(B.gcol[(x.sg >> 4) - 1] + v);
   return v + (uint32_t)x.base;
 }
 
@@ -103,7 +96,8 @@ __device__ __forceinline__ void bulk_g2s_hint(void* dst, const void* src, uint32
 
 // Starts the lookup of one row in a merged table: the entry's words are
 // copied to the row's slot of the group's region (zeros when the key is
-// outside the table).
+// outside the table).  Entries of 4 or 8 words go in 16-byte pieces, other
+// even widths in 8-byte pieces, odd widths word by word.
 __device__ __forceinline__ void fill_issue(const ProbeGroup& G, const int32_t* stage, uint32_t* mwb, int row,
                                            uint64_t pol) {
   const uint32_t off = (uint32_t)stage[G.col * kTileRows + row] - (uint32_t)G.key_min;
@@ -111,12 +105,12 @@ __device__ __forceinline__ void fill_issue(const ProbeGroup& G, const int32_t* s
   const int W = G.words;
   const uint32_t* src = G.table + (size_t)(in ? off : 0u) * W;
   uint32_t* dst = mwb + G.word_off * kTileRows + row * W;
-  if (W == 1) {
-    cp_async_zfill<4>(dst, src, in, pol);
-  } else if (W == 2) {
-    cp_async_zfill<8>(dst, src, in, pol);
-  } else {
+  if ((W & 3) == 0) {
     for (int h = 0; h < W; h += 4) cp_async_zfill<16>(dst + h, src + h, in, pol);
+  } else if ((W & 1) == 0) {
+    for (int h = 0; h < W; h += 2) cp_async_zfill<8>(dst + h, src + h, in, pol);
+  } else {
+    for (int h = 0; h < W; h++) cp_async_zfill<4>(dst + h, src + h, in, pol);
   }
 }
 
@@ -152,21 +146,21 @@ __device__ __forceinline__ void mquery_tile(const MQuery& Q, const BatchParams& 
   for (int r = 0; r < nr; r++) {
     const int live = __reduce_add_sync(0xffffffffu, __popc(m));
     if (!live) return;
-    const MRange R = Q.range[r];
-    const int32_t* cv = stage + R.col * kTileRows;
-    const uint32_t span = (uint32_t)R.hi - (uint32_t)R.lo;
+    const int32_t* cv = stage + Q.range_col[r] * kTileRows;
+    const uint32_t rlo = (uint32_t)Q.range_lo[r];
+    const uint32_t span = (uint32_t)Q.range_hi[r] - rlo;
     if (live > kDenseRows) {
       uint32_t keep = 0;
 #pragma unroll 8
       for (int i = 0; i < kChunks; i++) {
-        const uint32_t bb = __ballot_sync(0xffffffffu, (uint32_t)cv[32 * i + lane] - (uint32_t)R.lo <= span);
+        const uint32_t bb = __ballot_sync(0xffffffffu, (uint32_t)cv[32 * i + lane] - rlo <= span);
         keep = lane == i ? bb : keep;
       }
       m &= keep;
     } else {
       for (uint32_t bb = m; bb; bb &= bb - 1) {
         const int j = __ffs(bb) - 1;
-        if ((uint32_t)cv[r0 + j] - (uint32_t)R.lo > span) m &= ~(1u << j);
+        if ((uint32_t)cv[r0 + j] - rlo > span) m &= ~(1u << j);
       }
     }
   }
@@ -195,7 +189,7 @@ __device__ __forceinline__ void mquery_tile(const MQuery& Q, const BatchParams& 
 #pragma unroll
     for (int q = 0; q < kMaxKeys; q++) {
       if (q < nkeys) {
-        const uint32_t off = mx(kx[q], stage, mw, row);
+        const uint32_t off = mx(kx[q], B, stage, mw, row);
         in_range &= off < kr[q];
         gi += off * ks[q];
       }
@@ -207,11 +201,11 @@ __device__ __forceinline__ void mquery_tile(const MQuery& Q, const BatchParams& 
 #pragma unroll
     for (int mi = 0; mi < kMaxMetrics; mi++) {
       if (mi < nm) {
-        const uint32_t va = mx(xa[mi], stage, mw, row);
+        const uint32_t va = mx(xa[mi], B, stage, mw, row);
         uint32_t v = va;
         const int f = mf[mi];
         if (f != MF_OPND) {
-          const uint32_t vb = mx(xb[mi], stage, mw, row);
+          const uint32_t vb = mx(xb[mi], B, stage, mw, row);
           v = f == MF_ADD ? va + vb : f == MF_SUB ? va - vb : va * vb;
         }
         if (nkeys == 0)
@@ -232,12 +226,6 @@ __device__ __forceinline__ void mquery_tile(const MQuery& Q, const BatchParams& 
       }
     }
   }
-}
-
-__device__ __forceinline__ void copy_desc(MQuery* dst, const MQuery* src, int lane) {
-  if (lane < kDescChunks)
-    cp_async16(reinterpret_cast<uint4*>(dst) + lane, reinterpret_cast<const uint4*>(src) + lane);
-  cp_async_commit();
 }
 
 // The queries active on the tile starting at `tile_start` and the probe
@@ -274,8 +262,8 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
   int32_t* ring = reinterpret_cast<int32_t*>(dyn);
   uint32_t* mwbuf = reinterpret_cast<uint32_t*>(dyn + (size_t)nst * ncols * kTileRows * 4);  // two buffers
   uint32_t* bm = mwbuf + 2 * mw_words;
-  MQuery* dbuf = reinterpret_cast<MQuery*>(bm + kMaxMergedTables * kBmStride);
-  long long* qlo = reinterpret_cast<long long*>(dbuf + 2 * kMBatchWarps);
+  MQuery* sq = reinterpret_cast<MQuery*>(bm + kMaxMergedTables * kBmStride);  // every query's descriptor
+  long long* qlo = reinterpret_cast<long long*>(sq + nq);
   long long* qhi = qlo + nq;
   uint32_t* qg = reinterpret_cast<uint32_t*>(qhi + nq);
   uint16_t* act = reinterpret_cast<uint16_t*>(qg + nq);
@@ -290,6 +278,8 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
     }
     mbar_fence_init();
   }
+  for (int i = tid; i < nq * (int)(sizeof(MQuery) / 16); i += kMBThreads)
+    reinterpret_cast<uint4*>(sq)[i] = reinterpret_cast<const uint4*>(B.mq)[i];
   for (int q = tid; q < nq; q += kMBThreads) {
     qlo[q] = B.mq[q].row_begin;
     qhi[q] = B.mq[q].row_end;
@@ -365,11 +355,10 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
     // never waited for exists only after a timeout).
     if (tma && lane == 0 && last_real > last_seen)
       mbar_wait_bounded(&full[last_real % nst], (uint32_t)((last_real / nst) & 1), kPolls);
-    cp_async_wait<0>();
+    cp_async_wait_all();
     return;
   }
 
-  MQuery* mybuf = dbuf + 2 * warp;
   for (long long i = 0;; i++) {
     const int s = (int)(i % nst), b = (int)(i & 1);
     const uint32_t sp = (uint32_t)((i / nst) & 1), bp = (uint32_t)((i / 2) & 1);
@@ -408,32 +397,17 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
       if (lane < B.gtab0[g + 1] - t0) bm[(t0 + lane) * kBmStride + chunk] = present;
     }
     consumer_bar();
-    // Queries, claimed one at a time; the next one's descriptor is copied in
-    // while this one runs.
-    int k = 0;
-    if (lane == 0) k = atomicAdd(&s_next, 1);
-    k = __shfl_sync(0xffffffffu, k, 0);
-    if (k < na) copy_desc(mybuf, B.mq + act[k], lane);
-    int cur = 0;
-    while (k < na) {
-      int kn = 0;
-      if (lane == 0) kn = atomicAdd(&s_next, 1);
-      kn = __shfl_sync(0xffffffffu, kn, 0);
-      if (kn < na)
-        copy_desc(mybuf + (cur ^ 1), B.mq + act[kn], lane);
-      else
-        cp_async_commit();
-      cp_async_wait<1>();
-      __syncwarp();
+    // Queries, claimed one at a time.
+    for (;;) {
+      int k = 0;
+      if (lane == 0) k = atomicAdd(&s_next, 1);
+      k = __shfl_sync(0xffffffffu, k, 0);
+      if (k >= na) break;
       const int q = act[k];
       const long long lo = qlo[q] > tile_start ? qlo[q] - tile_start : 0;
       const long long hi = qhi[q] < tile_end ? qhi[q] - tile_start : kTileRows;
-      mquery_tile(mybuf[cur], B, stage, mw, bm, (int)lo, (int)hi, lane);
-      __syncwarp();
-      cur ^= 1;
-      k = kn;
+      mquery_tile(sq[q], B, stage, mw, bm, (int)lo, (int)hi, lane);
     }
-    cp_async_wait<0>();
     consumer_bar();
     if (tid == 0) {
       mbar_arrive(&empty[s]);
@@ -476,8 +450,7 @@ cudaError_t launch_merge_build(const MergeBuild& m, uint32_t* out, cudaStream_t 
 
 size_t mbatch_smem_bytes(const BatchParams& b) {
   return (size_t)b.nstages * b.ncols * kTileRows * 4 + 2 * (size_t)b.nmwords * kTileRows * 4 +
-         (size_t)kMaxMergedTables * kBmStride * 4 + sizeof(MQuery) * 2 * kMBatchWarps +
-         (size_t)b.nqueries * (8 + 8 + 4 + 2) + 16;
+         (size_t)kMaxMergedTables * kBmStride * 4 + (size_t)b.nqueries * (sizeof(MQuery) + 8 + 8 + 4 + 2) + 16;
 }
 
 int mbatch_grid_size(const BatchParams& b, size_t smem) {

@@ -736,6 +736,19 @@ __global__ void batch_write_kernel(const BatchQuery* Q, int nq, const unsigned l
   }
 }
 
+__global__ void batch_bounds_kernel(const BatchQuery* Q, int nq, const unsigned long long* pos,
+                                    unsigned long long total, unsigned long long* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= nq; i += gridDim.x * blockDim.x)
+    out[i] = pos[i < nq ? Q[i].group_off : total];
+}
+
+cudaError_t launch_batch_bounds(const BatchQuery* Q, int nq, const unsigned long long* pos, unsigned long long total,
+                                unsigned long long* out, cudaStream_t s) {
+  note_launch();
+  batch_bounds_kernel<<<(nq + 256) / 256, 256, 0, s>>>(Q, nq, pos, total, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_batch_finalize(const BatchQuery* Q, int nq, const unsigned long long* slots,
                                   unsigned long long total, uint32_t* flags, unsigned long long* pos,
                                   unsigned long long* scan_tmp, const BatchOut* out, cudaStream_t s) {

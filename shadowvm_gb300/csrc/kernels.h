@@ -90,6 +90,9 @@ cudaError_t launch_batch(const BatchParams& b, int grid, size_t smem, cudaStream
 // out == nullptr: flags (one per group of every query) and their exclusive
 // scan into pos (total + 1 entries); else write each flagged group's keys and
 // sums at pos into `out`.
+// out[i] = pos[Q[i].group_off] (the first result row of query i), out[nq] = pos[total].
+cudaError_t launch_batch_bounds(const BatchQuery* Q, int nq, const unsigned long long* pos, unsigned long long total,
+                                unsigned long long* out, cudaStream_t s);
 cudaError_t launch_batch_finalize(const BatchQuery* Q, int nq, const unsigned long long* slots,
                                   unsigned long long total, uint32_t* flags, unsigned long long* pos,
                                   unsigned long long* scan_tmp, const BatchOut* out, cudaStream_t s);

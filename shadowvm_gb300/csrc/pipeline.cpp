@@ -964,9 +964,7 @@ void plan_merge(const std::vector<BatchQuery>& qs, const std::vector<BatchItem>&
       ProbeGroup& G = mp->groups[g];
       G.key_min = (int32_t)kmin;
       G.span = (uint32_t)(kmax - kmin + 1);
-      int words = 1;
-      while (words < 1 + (int)freebits.size()) words *= 2;
-      G.words = words;
+      G.words = 1 + (int)freebits.size();
     }
   }
   // Groups beyond the per-row word or table-slot budget are left out (their
@@ -1088,8 +1086,20 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
   // ---- merged probe groups, and the queries they cover
   MergePlan mp;
   plan_merge(qs, items, &mp);
+  // Shared memory of the merged kernel without descriptors (two-stage ring);
+  // each query adds its resident descriptor.
+  const size_t kMergedSmem = 226 * 1024, kPerQuery = sizeof(MQuery) + 8 + 8 + 4 + 2;
+  auto merged_fixed = [&](int nst) {
+    BatchParams T{};
+    T.ncols = (int)ucols.size();
+    T.nstages = nst;
+    T.nmwords = mp.nmwords;
+    return mbatch_smem_bytes(T);
+  };
+  if (merged_fixed(2) + kPerQuery > kMergedSmem) mp.place.clear();  // every query takes the per-query kernel
   std::vector<int> order, legacy;
   std::vector<MQuery> mqs(nq);
+  std::vector<const int32_t*> gcols;
   for (int i = 0; i < nq; i++) {
     BatchQuery& Q = qs[i];
     struct DimPlace {
@@ -1118,23 +1128,29 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
     MQuery M{};
     M.row_begin = Q.row_begin;
     M.row_end = Q.row_end;
-    M.ngroups = Q.ngroups;
+    M.ngroups = (uint32_t)Q.ngroups;
+    bool fits = true;
     for (int k = 0; k < Q.nsteps; k++) {
       const Step& st = Q.steps[k];
       if (st.kind == STEP_PROBE) {
         const MergePlan::Place& pl = dp[st.dim].p;
         M.probe_tab[M.nprobe++] = (uint8_t)pl.slot;
-        M.tmask |= 1ull << pl.slot;
         M.gmask |= 1u << pl.group;
         if (st.lo == INT_MIN && st.hi == INT_MAX) continue;
       }
-      M.range[M.nrange++] = MRange{st.col, st.lo, st.hi};
+      if (M.nrange == kMaxMRanges) {
+        fits = false;
+        break;
+      }
+      M.range_col[M.nrange] = (uint8_t)st.col;
+      M.range_lo[M.nrange] = st.lo;
+      M.range_hi[M.nrange] = st.hi;
+      M.nrange++;
     }
     auto mxt = [&](const Extract& e) {
       MExtract r{};
       r.mask = e.mask;
       r.base = e.base;
-      r.col = e.col;
       if (e.dim < 0) {
         r.src = -1;
         r.slot = (uint8_t)e.slot;
@@ -1143,10 +1159,21 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
       // A payload field at bit `shift` of the entry sits at pay_bit + shift - 1
       // of the payload word (the present bit is not carried there).
       const MergePlan::Place& pl = dp[e.dim].p;
-      r.src = (int16_t)mp.groups[pl.group].word_off;
+      r.src = (int8_t)mp.groups[pl.group].word_off;
       r.slot = (uint8_t)pl.pay_word;
-      r.stride = mp.groups[pl.group].words;
+      r.sg = (uint8_t)mp.groups[pl.group].words;
       r.shift = (uint8_t)(pl.pay_bit + (e.mask ? e.shift - 1 : 0));
+      if (e.col) {
+        size_t gi = std::find(gcols.begin(), gcols.end(), e.col) - gcols.begin();
+        if (gi == gcols.size()) {
+          if (gcols.size() == (size_t)kMaxGatherCols) {
+            fits = false;
+            return r;
+          }
+          gcols.push_back(e.col);
+        }
+        r.sg |= (uint8_t)((gi + 1) << 4);
+      }
       M.gmask |= 1u << pl.group;
       return r;
     };
@@ -1161,6 +1188,11 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
       M.mform[m] = (uint8_t)Q.mform[m];
       M.xa[m] = mxt(Q.xa[m]);
       if (Q.mform[m] != MF_OPND) M.xb[m] = mxt(Q.xb[m]);
+    }
+    if (!fits) {  // more range steps or gather columns than the descriptor holds
+      order.pop_back();
+      legacy.push_back(i);
+      continue;
     }
     mqs[i] = M;
   }
@@ -1194,43 +1226,56 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
   x->scratch_reset();
   const size_t qbytes = sizeof(BatchQuery) * nq, mbytes = sizeof(MQuery) * nmerged;
   const size_t fin_words = (total_groups + 1) / 2 + 1 + total_groups + 1 + scan_tmp_words(total_groups);
-  const size_t need = qbytes + mbytes + 8 * slot_words + 16 + 8 * fin_words + 8 * 1024;
+  // Merged launches: as many queries per launch as their descriptors fit.
+  int mst = 2;
+  for (int nst = kStages; nst > 2; nst--)
+    if (merged_fixed(nst) + kPerQuery * nmerged <= kMergedSmem) {
+      mst = nst;
+      break;
+    }
+  const int per_launch = nmerged ? (int)((kMergedSmem - merged_fixed(mst)) / kPerQuery) : 1;
+  const int nlaunch = nmerged ? (nmerged + per_launch - 1) / per_launch : 0;
+  const size_t need = qbytes + mbytes + 8 * slot_words + 8 * (nlaunch + 1) + 8 * fin_words + 8 * (nq + 1) + 8 * 1024;
   if ((st = x->scratch_reserve(need))) return st;
-  void *dq, *dm = nullptr, *slots, *ctr, *fin;
+  void *dq, *dm = nullptr, *slots, *ctr, *fin, *bounds;
   if ((st = x->scratch_take(qbytes, &dq)) || (nmerged && (st = x->scratch_take(mbytes, &dm))) ||
-      (st = x->scratch_take(8 * slot_words, &slots)) || (st = x->scratch_take(16, &ctr)) ||
-      (st = x->scratch_take(8 * fin_words, &fin)))
+      (st = x->scratch_take(8 * slot_words, &slots)) || (st = x->scratch_take(8 * (nlaunch + 1), &ctr)) ||
+      (st = x->scratch_take(8 * fin_words, &fin)) || (st = x->scratch_take(8 * (nq + 1), &bounds)))
     return st;
   cudaError_t e = cudaMemcpyAsync(dq, dqs.data(), qbytes, cudaMemcpyHostToDevice, x->stream);
   if (!e && nmerged) e = cudaMemcpyAsync(dm, dmq.data(), mbytes, cudaMemcpyHostToDevice, x->stream);
   if (!e) e = cudaMemsetAsync(slots, 0, 8 * slot_words, x->stream);
-  if (!e) e = cudaMemsetAsync(ctr, 0, 16, x->stream);
+  if (!e) e = cudaMemsetAsync(ctr, 0, 8 * (nlaunch + 1), x->stream);
   if (e) return x->cuda_fail(e, "batch setup");
   cudaEvent_t ev;
-  for (int part = 0; part < 2; part++) {
-    const int q0 = part ? nmerged : 0, qn = part ? nq - nmerged : nmerged;
+  for (int part = 0; part <= nlaunch; part++) {
+    const bool merged = part < nlaunch;
+    const int q0 = merged ? part * per_launch : nmerged;
+    const int qn = merged ? std::min(per_launch, nmerged - q0) : nq - nmerged;
     if (!qn) continue;
     BatchParams B{};
     B.ncols = (int)ucols.size();
     for (size_t c = 0; c < ucols.size(); c++) B.cols[c] = (const int32_t*)ucols[c];
-    B.row_begin = lo[part];
-    B.row_end = std::max(hi[part], lo[part]);
+    long long rb = LLONG_MAX, re = LLONG_MIN;
+    for (int j = q0; j < q0 + qn; j++) {
+      rb = std::min(rb, dqs[j].row_begin);
+      re = std::max(re, dqs[j].row_end);
+    }
+    B.row_begin = rb;
+    B.row_end = std::max(re, rb);
     B.queries = (const BatchQuery*)dq + q0;
     B.nqueries = qn;
     B.slots = (unsigned long long*)slots;
     B.tile_counter = (unsigned long long*)ctr + part;
     B.error = x->d_error;
-    if (part == 0) {
+    if (merged) {
       B.nprobe = (int)mp.groups.size();
       for (size_t g = 0; g < mp.groups.size(); g++) B.probe[g] = mp.groups[g];
       B.nmwords = mp.nmwords;
-      B.mq = (const MQuery*)dm;
+      B.mq = (const MQuery*)dm + q0;
       for (size_t g = 0; g < mp.gtab0.size(); g++) B.gtab0[g] = mp.gtab0[g];
-      B.nstages = 2;
-      for (int nst = kStages; nst >= 2; nst--) {
-        B.nstages = nst;
-        if (mbatch_smem_bytes(B) <= 226 * 1024) break;
-      }
+      for (size_t c = 0; c < gcols.size(); c++) B.gcol[c] = gcols[c];
+      B.nstages = mst;
       const size_t smem = mbatch_smem_bytes(B);
       const int grid = mbatch_grid_size(B, smem);
       if (grid <= 0) {
@@ -1265,12 +1310,14 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
   x->prof_begin(SVM_K_FINALIZE, &ev);
   e = launch_batch_finalize(dQ, nq, (unsigned long long*)slots, total_groups, flags, pos, scant, nullptr, x->stream);
   x->prof_end(SVM_K_FINALIZE, ev);
-  std::vector<unsigned long long> hpos(total_groups + 1);
-  if (!e) e = cudaMemcpyAsync(hpos.data(), pos, 8 * (total_groups + 1), cudaMemcpyDeviceToHost, x->stream);
+  // Only each query's first result row comes back to the host.
+  std::vector<unsigned long long> hb(nq + 1);
+  if (!e) e = launch_batch_bounds(dQ, nq, pos, total_groups, (unsigned long long*)bounds, x->stream);
+  if (!e) e = cudaMemcpyAsync(hb.data(), bounds, 8 * (nq + 1), cudaMemcpyDeviceToHost, x->stream);
   if (e) return x->cuda_fail(e, "batch finalize");
   if ((st = sync_and_check(x, "batch"))) return st;
   // One result store for the batch; each query's rows are a slice of it.
-  const unsigned long long rows = hpos[total_groups];
+  const unsigned long long rows = hb[nq];
   std::vector<int> types = {SVM_INT32, SVM_INT32, SVM_INT32, SVM_INT64, SVM_INT64, SVM_INT64};
   ObjectPtr all = new_result_object(x, "", types, rows, &st);
   if (st) return st;
@@ -1292,8 +1339,8 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
     out->types = it.plan.out_types;
     for (int k = 0; k < Q.nkeys; k++) out->storage.push_back(all->storage[k]);
     for (int m = 0; m < Q.nmetrics; m++) out->storage.push_back(all->storage[kMaxKeys + m]);
-    out->row0 = hpos[Q.group_off];
-    out->nrows = hpos[Q.group_off + Q.ngroups] - out->row0;
+    out->row0 = hb[j];
+    out->nrows = hb[j + 1] - out->row0;
     out->has_bulks = true;
     out->bulk0_rows = out->nrows;
     out->source_rows = out->nrows;

@@ -183,7 +183,7 @@ constexpr int kMBatchWarps = 16;      // consumer warps of the merged batch kern
 
 struct ProbeGroup {
   int col;                  // union fact column slot of the key
-  int words;                // 1, 2, 4 or 8 words per key
+  int words;                // 1..8 words per key
   int32_t key_min;
   uint32_t span;
   int word_off;             // first merged word of the group in the per-row layout
@@ -208,35 +208,38 @@ struct MergeBuild {
   MergeSrc src[kMaxMergeSrcs];
 };
 
-// The merged kernel's own compact query descriptor (prefetched per warp).
-// Probe steps are bit tests against per-tile row bitmaps of the merged tables'
-// present bits (table slots 0..63); range steps test staged fact values.
+// The merged kernel's own compact query descriptor, held in shared memory
+// for the whole launch.  Probe steps are bit tests against per-tile row
+// bitmaps of the merged tables' present bits (table slots 0..63); range
+// steps test staged fact values.
 constexpr int kMaxMergedTables = 64;
+constexpr int kMaxMRanges = 6;
+constexpr int kMaxGatherCols = 15;
 
-struct MExtract {
-  int16_t src;          // -1: fact column `slot`; else the group's first merged word
-  uint8_t slot, shift;  // merged: `slot` = word within the group's entry
+struct MExtract {       // 12 bytes
+  int8_t src;           // -1: fact column `slot`; else the group's first merged word
+  uint8_t slot;         // fact column slot, or the word within the group's entry
+  uint8_t shift;
+  uint8_t sg;           // merged: words per row (low 4 bits); gather column + 1 (high 4 bits, 0 = none)
   uint32_t mask;
-  int32_t base;
-  int32_t stride;       // merged: the group's words per row
-  const int32_t* col;   // non-null: value = col[field] + base
+  int32_t base;         // value = field (or gcol[field]) + base
 };
 
-struct MRange {
-  int32_t col, lo, hi;
-};
-
-struct MQuery {
+struct MQuery {         // 240 bytes
   long long row_begin, row_end;
-  unsigned long long slot_off, ngroups;
-  unsigned long long tmask;         // table slots the query tests
+  unsigned long long slot_off;
+  uint32_t ngroups;
   uint32_t gmask;                   // probe groups whose words it reads
   uint8_t nprobe, nrange, nkeys, nmetrics;
+  uint8_t mform[kMaxMetrics];
+  uint8_t pad0;
   uint8_t probe_tab[kMaxSteps];
-  uint8_t mform[4];
+  uint8_t range_col[kMaxMRanges];
+  uint8_t pad1[2];
+  int32_t range_lo[kMaxMRanges], range_hi[kMaxMRanges];
   uint32_t krange[kMaxKeys], kstride[kMaxKeys];
-  MRange range[kMaxSteps];
   MExtract kx[kMaxKeys], xa[kMaxMetrics], xb[kMaxMetrics];
+  uint32_t pad2;
 };
 
 struct BatchQuery {                 // in device memory, one per query
@@ -272,6 +275,7 @@ struct BatchParams {
   int nmwords;                      // merged words per row
   const MQuery* mq;                 // merged kernel: descriptors (nqueries)
   int gtab0[kMaxProbeGroups + 1];   // group g's tables are slots [gtab0[g], gtab0[g + 1]), in present-bit order
+  const int32_t* gcol[kMaxGatherCols];  // row-index payload columns (MExtract::sg high bits)
 };
 
 // Fills the flattened copies (Step table fields, Extract descriptors) from the

@@ -140,16 +140,17 @@ class Engine:
         self._check(self.lib.svm_object_drop(self.h, oid.encode()))
 
     # ------------------------------------------------------------ pipelines
-    def run(self, pipe: PipelineInfo):
-        """RunPipelineCMD: the output is stored as object `pipe.id`."""
-        keep = []
-        p = marshal(pipe, keep)
-        self._check(self.lib.svm_run_pipeline(self.h, ctypes.byref(p)))
+    def run(self, pipe):
+        """RunPipelineCMD: the output is stored as object `pipe.id`.  `pipe` is
+        a PipelineInfo or a Prepared one (marshalled once, run many times)."""
+        p = pipe if isinstance(pipe, Prepared) else Prepared([pipe])
+        self._check(self.lib.svm_run_pipeline(self.h, ctypes.byref(p.arr[0])))
 
-    def run_batch(self, pipes: list[PipelineInfo]):
-        keep = []
-        arr = (capi.svm_pipeline * max(len(pipes), 1))(*[marshal(p, keep) for p in pipes])
-        self._check(self.lib.svm_run_batch(self.h, len(pipes), arr))
+    def run_batch(self, pipes):
+        """Many pipelines in one call (svm_run_batch); a list of PipelineInfo
+        or a Prepared batch."""
+        p = pipes if isinstance(pipes, Prepared) else Prepared(pipes)
+        self._check(self.lib.svm_run_batch(self.h, p.n, p.arr))
 
     def result(self, oid: str, key_num: int) -> tuple[np.ndarray, np.ndarray]:
         """A reduce pipeline's output: keys int32 [g, key_num], sums int64 [g, m]."""
@@ -180,6 +181,16 @@ def capi_type(dtype) -> int:
     if dt == np.int64:
         return int(ValType.Int64)
     raise TypeError(f"unsupported column dtype {dt}")
+
+
+class Prepared:
+    """Pipelines marshalled into C-ABI structs once (as a server decodes a
+    request once), reusable across run / run_batch calls."""
+
+    def __init__(self, pipes: list[PipelineInfo]):
+        self.keep = []
+        self.n = len(pipes)
+        self.arr = (capi.svm_pipeline * max(self.n, 1))(*[marshal(p, self.keep) for p in pipes])
 
 
 def marshal(pipe: PipelineInfo, keep: list) -> capi.svm_pipeline:

@@ -122,3 +122,17 @@ def test_batch_full_range_and_overlaps(engine_factory):
     for i in one:
         np.testing.assert_array_equal(many[i][0], one[i][0])
         np.testing.assert_array_equal(many[i][1], one[i][1])
+
+
+def test_batch_larger_than_one_launch(engine_factory):
+    """More queries than one merged launch keeps in shared memory: the batch
+    is split over several launches with the same results."""
+    bw = W.make_batch(700, qseed=21, **SMALL)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk)
+    W.load_batch(eng, bw)
+    idx = list(range(0, 700, 7))
+    one = singles(eng, bw, idx)
+    many = batched(eng, bw)
+    for i in idx:
+        np.testing.assert_array_equal(many[i][0], one[i][0], err_msg=f"keys of query {i}")
+        np.testing.assert_array_equal(many[i][1], one[i][1], err_msg=f"sums of query {i}")
