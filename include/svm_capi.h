@@ -21,6 +21,7 @@
  *                                 ReduceTask (core/pipeline.cu:360-472); result cached by pipeline
  *                                 id like ShadowVMService::cached_obj (service/service.hpp:92)
  *   svm_run_batch                 no counterpart: many RunPipelineCMD calls folded into one launch
+ *   svm_pipeline_footprint        no counterpart: device bytes a pipeline needs (served admission)
  */
 #ifndef SVM_CAPI_H_
 #define SVM_CAPI_H_
@@ -73,7 +74,12 @@ typedef struct svm_config {
   int join_mode;                     /* SVM_JOIN_REF_COMPAT (default) or SVM_JOIN_EXACT */
   int hash_char_signed;              /* 1 (default): hash key bytes as signed char, as the
                                         x86 reference does; 0: unsigned (aarch64 build) */
+  int batch_policy;                  /* svm_run_batch: SVM_BATCH_AUTO (default) picks the cheaper
+                                        of one shared launch and per-query launches by a cost
+                                        model; SVM_BATCH_ALWAYS / SVM_BATCH_NEVER force one */
 } svm_config;
+
+enum { SVM_BATCH_AUTO = 0, SVM_BATCH_ALWAYS = 1, SVM_BATCH_NEVER = 2 };
 
 typedef struct svm_ctx svm_ctx;
 
@@ -116,6 +122,16 @@ svm_status svm_object_read(svm_ctx* ctx, const char* id, int col, unsigned long 
                            unsigned long long n, void* host_out);
 /* Device address of column `col` (valid until the object is dropped/replaced). */
 svm_status svm_object_device_ptr(svm_ctx* ctx, const char* id, int col, void** dptr);
+/* Several whole objects to host memory in one device pass (one gather kernel,
+ * one copy, one synchronisation).  For each object in order and each of its
+ * columns in order, the column's rows are written to `host` starting at an
+ * 8-byte-aligned offset (int32 columns take 4 bytes a row, int64 8).
+ * nrows_out[k] gets object k's row count and *needed the total bytes; with
+ * host == NULL only those are returned.  No counterpart in the reference (its
+ * wire has no result fetch); the served loop reads a fold's results with it. */
+svm_status svm_objects_read(svm_ctx* ctx, int n, const char* const* ids, void* host, unsigned long long cap,
+                            unsigned long long* nrows_out, unsigned long long* needed);
+
 svm_status svm_object_drop(svm_ctx* ctx, const char* id);
 
 /* ---- pipelines (PipelineInfo, com/svm.proto:101-144) ---------------------- */
@@ -161,6 +177,13 @@ svm_status svm_run_pipeline(svm_ctx* ctx, const svm_pipeline* pipe);
  * Every output is stored as in svm_run_pipeline.  The result of each pipeline
  * equals its result from svm_run_pipeline. */
 svm_status svm_run_batch(svm_ctx* ctx, int n, const svm_pipeline* pipes);
+
+/* Device bytes that running `pipe` needs beyond what is resident (group
+ * slots, finalize scratch and the largest possible result), for admission by
+ * HBM footprint.  Plans the pipeline; dimension tables it joins are built and
+ * cached as svm_run_pipeline would.  No counterpart in the reference (it has
+ * no admission control, service/service.cu:25-63). */
+svm_status svm_pipeline_footprint(svm_ctx* ctx, const svm_pipeline* pipe, unsigned long long* bytes);
 
 /* ---- allocation-free scan ---------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

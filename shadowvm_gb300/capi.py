@@ -25,7 +25,7 @@ K_STAR, K_SELECT, K_BUILD, K_FINALIZE, K_BATCH, K_OTHER, K_COUNT = range(7)
 class svm_config(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_ulonglong),
                 ("tuple_per_bulk", ctypes.c_ulonglong), ("join_mode", ctypes.c_int),
-                ("hash_char_signed", ctypes.c_int)]
+                ("hash_char_signed", ctypes.c_int), ("batch_policy", ctypes.c_int)]
 
 
 class svm_arg(ctypes.Structure):
@@ -104,8 +104,10 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "svm_object_read": (I, [P, cp, I, U64, U64, P]),
         "svm_object_device_ptr": (I, [P, cp, I, ctypes.POINTER(P)]),
         "svm_object_drop": (I, [P, cp]),
+        "svm_objects_read": (I, [P, I, ctypes.POINTER(cp), P, U64, ctypes.POINTER(U64), ctypes.POINTER(U64)]),
         "svm_run_pipeline": (I, [P, ctypes.POINTER(svm_pipeline)]),
         "svm_run_batch": (I, [P, I, ctypes.POINTER(svm_pipeline)]),
+        "svm_pipeline_footprint": (I, [P, ctypes.POINTER(svm_pipeline), ctypes.POINTER(U64)]),
         "svm_profile_enable": (I, [P, I]),
         "svm_profile_reset": (I, [P]),
         "svm_profile_read": (I, [P, I, ctypes.POINTER(U64), ctypes.POINTER(D)]),

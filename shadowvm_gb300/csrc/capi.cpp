@@ -1,4 +1,5 @@
 // The C ABI (include/svm_capi.h): context, object store, profiling.
+#include <algorithm>
 #include <climits>
 #include <cstring>
 
@@ -86,6 +87,21 @@ svm_status Ctx::alloc(size_t bytes, DevBufPtr* out, bool zero) {
   in_use += bytes;
   if (zero && (e = cudaMemsetAsync(b->p, 0, bytes, stream)) != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   *out = b;
+  return SVM_OK;
+}
+
+svm_status Ctx::pinned_reserve(size_t bytes) {
+  if (pinned_bytes >= bytes) return SVM_OK;
+  if (pinned) cudaFreeHost(pinned);
+  pinned = nullptr;
+  pinned_bytes = 0;
+  size_t want = std::max(bytes, pinned_bytes * 2);
+  cudaError_t e = cudaMallocHost(&pinned, want);
+  if (e) {
+    pinned = nullptr;
+    return cuda_fail(e, "cudaMallocHost");
+  }
+  pinned_bytes = want;
   return SVM_OK;
 }
 
@@ -189,6 +205,7 @@ void svm_config_default(svm_config* cfg) {
   cfg->tuple_per_bulk = 2000000ull;  // com/cpp/com.cu:13
   cfg->join_mode = SVM_JOIN_REF_COMPAT;
   cfg->hash_char_signed = 1;
+  cfg->batch_policy = SVM_BATCH_AUTO;
 }
 
 svm_status svm_init(const svm_config* cfg, svm_ctx** out) {
@@ -232,6 +249,7 @@ void svm_destroy(svm_ctx* c) {
   x->dim_cache.clear();
   x->scratch.reset();
   x->trim_pool(0);
+  if (x->pinned) cudaFreeHost(x->pinned);
   for (auto e : x->event_pool) cudaEventDestroy(e);
   if (x->d_error) cudaFree(x->d_error);
   if (x->stream) cudaStreamDestroy(x->stream);
@@ -405,14 +423,60 @@ svm_status svm_object_drop(svm_ctx* c, const char* id) {
   if (it == x->objects.end()) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
   cudaStreamSynchronize(x->stream);
   x->objects.erase(it);
-  // Tables built over the dropped object are keyed by its version; drop them too.
-  x->merged_cache.clear();
+  // Tables built over the dropped object are keyed by its version; drop them
+  // too, with the merged probe tables made from them.
+  std::vector<const svm::DimTable*> gone;
   for (auto d = x->dim_cache.begin(); d != x->dim_cache.end();) {
-    if (d->first.compare(0, std::strlen(id) + 1, std::string(id) + "#") == 0)
+    if (d->first.compare(0, std::strlen(id) + 1, std::string(id) + "#") == 0) {
+      gone.push_back(d->second.get());
       d = x->dim_cache.erase(d);
-    else
+    } else {
       ++d;
+    }
   }
+  if (!gone.empty())
+    for (auto m = x->merged_cache.begin(); m != x->merged_cache.end();) {
+      bool hit = false;
+      for (const svm::DimTablePtr& t : m->second.srcs) hit |= std::find(gone.begin(), gone.end(), t.get()) != gone.end();
+      m = hit ? x->merged_cache.erase(m) : std::next(m);
+    }
+  return SVM_OK;
+}
+
+svm_status svm_objects_read(svm_ctx* c, int n, const char* const* ids, void* host, unsigned long long cap,
+                            unsigned long long* nrows_out, unsigned long long* needed) {
+  if (!c || n < 0 || (n && (!ids || !nrows_out)) || !needed) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  cudaSetDevice(x->device);
+  x->err.clear();
+  std::vector<svm::Segment> segs;
+  unsigned long long total = 0;  // bytes; every column starts 8-byte aligned
+  for (int k = 0; k < n; k++) {
+    ObjectPtr o = ids[k] ? x->find(ids[k]) : nullptr;
+    if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + (ids[k] ? ids[k] : "(null)"));
+    nrows_out[k] = o->nrows;
+    for (int col = 0; col < o->ncols; col++) {
+      const unsigned long long bytes = o->nrows * o->elem(col);
+      if (bytes) segs.push_back(svm::Segment{(const uint32_t*)o->col(col), total / 4, bytes / 4});
+      total += (bytes + 7) & ~7ull;
+    }
+  }
+  *needed = total;
+  if (!host || !total) return SVM_OK;
+  if (cap < total) return x->fail(SVM_E_INVALID_ARG, "objects read: host buffer smaller than needed bytes");
+  x->scratch_reset();
+  const size_t sbytes = segs.size() * sizeof(svm::Segment);
+  svm_status st = x->scratch_reserve(sbytes + total + 1024);
+  void *dseg, *dbuf;
+  if (st || (st = x->scratch_take(sbytes, &dseg)) || (st = x->scratch_take(total, &dbuf))) return st;
+  if ((st = x->pinned_reserve(total))) return st;
+  cudaError_t e = cudaMemcpyAsync(dseg, segs.data(), sbytes, cudaMemcpyHostToDevice, x->stream);
+  if (!e) e = svm::launch_gather_segments((const svm::Segment*)dseg, (int)segs.size(), (uint32_t*)dbuf, x->stream);
+  if (!e) e = cudaMemcpyAsync(x->pinned, dbuf, total, cudaMemcpyDeviceToHost, x->stream);
+  if (!e) e = cudaStreamSynchronize(x->stream);
+  if (e) return x->cuda_fail(e, "objects read");
+  std::memcpy(host, x->pinned, total);
   return SVM_OK;
 }
 
@@ -432,6 +496,16 @@ svm_status svm_run_batch(svm_ctx* c, int n, const svm_pipeline* p) {
   cudaSetDevice(x->device);
   x->err.clear();
   return svm::run_batch(x, n, p);
+}
+
+svm_status svm_pipeline_footprint(svm_ctx* c, const svm_pipeline* p, unsigned long long* bytes) {
+  if (!c || !p || !bytes) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  cudaSetDevice(x->device);
+  x->err.clear();
+  *bytes = 0;
+  return svm::pipeline_footprint(x, p, bytes);
 }
 
 unsigned long long svm_kernel_launches(void) { return svm::launches_total(); }

@@ -95,6 +95,9 @@ struct Ctx {
   // class; charged to the budget until trimmed.
   std::multimap<size_t, void*> pool;
   size_t pooled = 0;
+  // Pinned host staging for bulk reads (grows, kept).
+  void* pinned = nullptr;
+  size_t pinned_bytes = 0;
   unsigned long long next_version = 1;
   std::map<std::string, ObjectPtr> objects;
   std::map<std::string, DimTablePtr> dim_cache;
@@ -120,6 +123,7 @@ struct Ctx {
   // Allocation charged to the budget (zero-filled when `zero`).
   svm_status alloc(size_t bytes, DevBufPtr* out, bool zero = false);
   void release(void* p, size_t bytes);        // a DevBuf's block: back to the pool or freed
+  svm_status pinned_reserve(size_t bytes);
   void trim_pool(size_t keep);                // frees pooled blocks until at most `keep` bytes stay
   // Scratch: reset() then take() pieces; valid until the next reset().
   void scratch_reset() { scratch_used = 0; }
@@ -140,6 +144,7 @@ struct Ctx {
 // Pipelines (pipeline.cpp).
 svm_status run_pipeline(Ctx* ctx, const svm_pipeline* p);
 svm_status run_batch(Ctx* ctx, int n, const svm_pipeline* p);
+svm_status pipeline_footprint(Ctx* ctx, const svm_pipeline* p, unsigned long long* bytes);
 
 }  // namespace svm
 

@@ -200,4 +200,24 @@ cudaError_t launch_inclusive_max(const int32_t* in, unsigned long long n, int32_
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- segment gather
+// One warp per segment (grid-stride over segments), consecutive lanes on
+// consecutive words.
+__global__ void gather_segments_kernel(const Segment* segs, int nseg, uint32_t* dst) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nseg; k += warps) {
+    const Segment sg = segs[k];
+    for (unsigned long long w = lane; w < sg.words; w += 32) dst[sg.dst_word + w] = sg.src[w];
+  }
+}
+
+cudaError_t launch_gather_segments(const Segment* segs, int nseg, uint32_t* dst, cudaStream_t s) {
+  if (nseg <= 0) return cudaSuccess;
+  const int blocks = (nseg + 7) / 8 < num_sms() * 8 ? (nseg + 7) / 8 : num_sms() * 8;
+  note_launch();
+  gather_segments_kernel<<<blocks, 256, 0, s>>>(segs, nseg, dst);
+  return cudaGetLastError();
+}
+
 }  // namespace svm

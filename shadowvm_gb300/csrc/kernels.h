@@ -31,6 +31,14 @@ cudaError_t launch_inclusive_max(const int32_t* in, unsigned long long n, int32_
                                  int32_t* tmp, cudaStream_t s);
 size_t max_tmp_words(unsigned long long n);
 
+// Copies `words` 32-bit words from `src` to dst + dst_word for every segment.
+struct Segment {
+  const uint32_t* src;
+  unsigned long long dst_word;
+  unsigned long long words;
+};
+cudaError_t launch_gather_segments(const Segment* segs, int nseg, uint32_t* dst, cudaStream_t s);
+
 // ---- select pipelines (kern_dim.cu)
 // Pass 1: per-tile counts of rows passing the conjuncts; pass 2: order-preserving write.
 unsigned long long select_tiles(long long nrows);

@@ -16,7 +16,7 @@ class Engine:
     """One data-plane context on one GPU."""
 
     def __init__(self, device: int = 0, tuple_per_bulk: int = 2_000_000, join_mode: str = "ref_compat",
-                 hbm_budget_bytes: int = 0, hash_char_signed: bool = True):
+                 hbm_budget_bytes: int = 0, hash_char_signed: bool = True, batch_policy: str = "auto"):
         self.lib = capi.load()
         cfg = capi.svm_config()
         self.lib.svm_config_default(ctypes.byref(cfg))
@@ -25,6 +25,7 @@ class Engine:
         cfg.join_mode = {"ref_compat": capi.JOIN_REF_COMPAT, "exact": capi.JOIN_EXACT}[join_mode]
         cfg.hbm_budget_bytes = hbm_budget_bytes
         cfg.hash_char_signed = int(hash_char_signed)
+        cfg.batch_policy = {"auto": 0, "always": 1, "never": 2}[batch_policy]
         h = ctypes.c_void_p()
         st = self.lib.svm_init(ctypes.byref(cfg), ctypes.byref(h))
         if st != capi.OK:
@@ -131,6 +132,30 @@ class Engine:
         nc, _ = self.info(oid)
         return [self.read(oid, c) for c in range(nc)]
 
+    def read_objects(self, oids: list[str], types: list[list[int]]) -> list[list[np.ndarray]]:
+        """Whole objects in one device pass (svm_objects_read); types[k] lists
+        object k's column types (ValType.Int32 / Int64)."""
+        n = len(oids)
+        if n == 0:
+            return []
+        ids = (ctypes.c_char_p * n)(*[o.encode() for o in oids])
+        rows = (ctypes.c_ulonglong * n)()
+        need = ctypes.c_ulonglong()
+        self._check(self.lib.svm_objects_read(self.h, n, ids, None, 0, rows, ctypes.byref(need)))
+        buf = np.empty(max(need.value, 8), np.uint8)
+        self._check(self.lib.svm_objects_read(self.h, n, ids, buf.ctypes.data_as(ctypes.c_void_p), buf.nbytes, rows,
+                                              ctypes.byref(need)))
+        out, off = [], 0
+        for k in range(n):
+            cols = []
+            for t in types[k]:
+                dt = np.int64 if t == ValType.Int64 else np.int32
+                nb = rows[k] * np.dtype(dt).itemsize
+                cols.append(buf[off:off + nb].view(dt).copy())
+                off += (nb + 7) & ~7
+            out.append(cols)
+        return out
+
     def device_ptr(self, oid: str, col: int) -> int:
         p = ctypes.c_void_p()
         self._check(self.lib.svm_object_device_ptr(self.h, oid.encode(), col, ctypes.byref(p)))
@@ -151,6 +176,14 @@ class Engine:
         or a Prepared batch."""
         p = pipes if isinstance(pipes, Prepared) else Prepared(pipes)
         self._check(self.lib.svm_run_batch(self.h, p.n, p.arr))
+
+    def footprint(self, pipe) -> int:
+        """Device bytes running `pipe` needs beyond what is resident (plans it;
+        joined dimension tables are built and cached)."""
+        p = pipe if isinstance(pipe, Prepared) else Prepared([pipe])
+        b = ctypes.c_ulonglong()
+        self._check(self.lib.svm_pipeline_footprint(self.h, ctypes.byref(p.arr[0]), ctypes.byref(b)))
+        return b.value
 
     def result(self, oid: str, key_num: int) -> tuple[np.ndarray, np.ndarray]:
         """A reduce pipeline's output: keys int32 [g, key_num], sums int64 [g, m]."""

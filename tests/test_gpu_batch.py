@@ -33,7 +33,7 @@ def batched(eng, bw, idx=None):
 @pytest.mark.parametrize("mode", ["ref_compat", "exact"])
 def test_batch_equals_one_launch_per_query(engine_factory, mode):
     bw = W.make_batch(64, qseed=11, **SMALL)
-    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, join_mode=mode)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, join_mode=mode, batch_policy="always")
     W.load_batch(eng, bw)
     one = singles(eng, bw)
     first = batched(eng, bw)  # builds and caches the merged probe tables
@@ -53,7 +53,7 @@ def test_batch_equals_one_launch_per_query(engine_factory, mode):
 
 def test_batch_exact_equals_numpy(engine_factory):
     bw = W.make_batch(24, qseed=5, **SMALL)
-    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, join_mode="exact")
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, join_mode="exact", batch_policy="always")
     W.load_batch(eng, bw)
     got = batched(eng, bw)
     fact = bw.fact.fact_host(0, bw.fact.fact_rows)
@@ -68,7 +68,7 @@ def test_batch_mixed_with_selects_and_unbatchable(engine_factory):
     kernel does not take (int32 sums, a division) runs alone; empty filters
     and empty views keep their single-query results."""
     bw = W.make_batch(12, qseed=3, **SMALL)
-    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, batch_policy="always")
     W.load_batch(eng, bw, build_dims=False)
     schema = bw.fact.fact_schema()
     extra = [
@@ -115,7 +115,7 @@ def test_batch_full_range_and_overlaps(engine_factory):
     spans = [(0, n), (0, n), (1, n - 1), (1023, 1), (1024, 1025), (n - 1, 1), (777, 3_333), (5, 2_000_000)]
     for q, (r0, ln) in zip(bw.queries, spans):
         q.row0, q.nrows = r0, ln
-    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, batch_policy="always")
     W.load_batch(eng, bw)
     one = singles(eng, bw)
     many = batched(eng, bw)
@@ -128,7 +128,7 @@ def test_batch_larger_than_one_launch(engine_factory):
     """More queries than one merged launch keeps in shared memory: the batch
     is split over several launches with the same results."""
     bw = W.make_batch(700, qseed=21, **SMALL)
-    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, batch_policy="always")
     W.load_batch(eng, bw)
     idx = list(range(0, 700, 7))
     one = singles(eng, bw, idx)
@@ -136,3 +136,74 @@ def test_batch_larger_than_one_launch(engine_factory):
     for i in idx:
         np.testing.assert_array_equal(many[i][0], one[i][0], err_msg=f"keys of query {i}")
         np.testing.assert_array_equal(many[i][1], one[i][1], err_msg=f"sums of query {i}")
+
+
+def test_served_loop_results_equal_alone(engine_factory):
+    """Requests arriving from several threads are folded into batched
+    launches by the served loop; each result equals the query run alone."""
+    import threading
+
+    from shadowvm_gb300 import serving
+    bw = W.make_batch(96, qseed=17, **SMALL)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, batch_policy="always")
+    W.load_batch(eng, bw)
+    alone = singles(eng, bw)
+    futs = {}
+    with serving.BatchLoop(eng, fetch=True, drop_results=True) as loop:
+        def client(k):
+            for i in range(k, len(bw.queries), 4):
+                q = bw.queries[i]
+                p = fact_pipeline(f"srv{i}", f"lo_q{i}", bw.fact.fact_schema(), q.pipe.pre_pipeline_id[1:],
+                                  [(o.args["lkey"], o.args["rkey"]) for o in q.pipe.workflow if "lkey" in o.args],
+                                  next(o.args["dim"] for o in q.pipe.workflow if "dim" in o.args),
+                                  next(o.args["metric"] for o in q.pipe.workflow if "metric" in o.args),
+                                  predication=next((o.args["predication"] for o in q.pipe.workflow
+                                                    if "predication" in o.args), None))
+                futs[i] = loop.submit(p, q.key_num)
+        ts = [threading.Thread(target=client, args=(k,)) for k in range(4)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        got = {i: f.result(timeout=120) for i, f in futs.items()}
+    assert max(loop.folds) > 1
+    for i in alone:
+        np.testing.assert_array_equal(got[i][0], alone[i][0], err_msg=f"keys of query {i}")
+        np.testing.assert_array_equal(got[i][1], alone[i][1], err_msg=f"sums of query {i}")
+
+
+def test_objects_read_matches_single_reads(engine_factory):
+    from shadowvm_gb300.serving import sink_types, split_result
+    bw = W.make_batch(20, qseed=23, **SMALL)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, batch_policy="always")
+    W.load_batch(eng, bw)
+    many = batched(eng, bw)
+    cols = eng.read_objects([q.pipe.id for q in bw.queries], [sink_types(q.pipe) for q in bw.queries])
+    for i, q in enumerate(bw.queries):
+        k, s = split_result(cols[i], q.key_num)
+        np.testing.assert_array_equal(k, many[i][0])
+        np.testing.assert_array_equal(s, many[i][1])
+
+
+@pytest.mark.parametrize("policy", ["never", "auto"])
+def test_batch_policy(engine_factory, policy):
+    """NEVER runs one launch per query, AUTO picks by the cost model; the
+    results are the same either way."""
+    from shadowvm_gb300 import capi
+    bw = W.make_batch(6, qseed=29, **SMALL)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, batch_policy=policy)
+    W.load_batch(eng, bw)
+    one = singles(eng, bw)
+    eng.profile(True)
+    eng.profile_reset()
+    many = batched(eng, bw)
+    n_batch, _ = eng.profile_read(capi.K_BATCH)
+    n_star, _ = eng.profile_read(capi.K_STAR)
+    eng.profile(False)
+    if policy == "never":
+        assert n_batch == 0 and n_star == 6
+    else:
+        assert (n_batch, n_star) in ((1, 0), (0, 6))
+    for i in one:
+        np.testing.assert_array_equal(many[i][0], one[i][0])
+        np.testing.assert_array_equal(many[i][1], one[i][1])
