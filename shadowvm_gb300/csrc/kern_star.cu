@@ -42,10 +42,26 @@ struct StarSmem {
 // A consumer warp's selection vector: surviving row offsets (within the
 // warp's 128 rows), and per probed dimension the matched table entry of each
 // row, indexed by row offset (so compaction only moves the offsets).
+// A consumer warp's selection vector in shared memory: the row indices of
+// its live rows and, per joined dimension, the probe word of each row.
 struct WarpList {
-  uint32_t pw[kMaxDims][kWarpRows];
-  uint16_t row[kWarpRows];
+  uint32_t* pwb;  // ndims x kWarpRows
+  uint16_t* row;  // kWarpRows
+  __device__ __forceinline__ uint32_t* pw(int d) const { return pwb + d * kWarpRows; }
 };
+
+// Bytes of one warp's list for `ndims` joined dimensions (16-byte multiple).
+__host__ __device__ __forceinline__ size_t warp_list_bytes(int ndims) {
+  return (size_t)(ndims > 0 ? ndims : 1) * kWarpRows * 4 + kWarpRows * 2;
+}
+
+__device__ __forceinline__ WarpList warp_list(uint8_t* base, int warp, int ndims) {
+  uint8_t* p = base + (size_t)warp * warp_list_bytes(ndims);
+  WarpList L;
+  L.pwb = reinterpret_cast<uint32_t*>(p);
+  L.row = reinterpret_cast<uint16_t*>(p + (size_t)(ndims > 0 ? ndims : 1) * kWarpRows * 4);
+  return L;
+}
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
@@ -129,6 +145,17 @@ __device__ __forceinline__ int32_t metric_value(const StarParams& P, const Metri
   return (int32_t)(a * b);
 }
 
+// 64-bit add into shared memory with two 32-bit atomics: the low word's
+// atomic returns its exact old value, so its carry is exact, and the high
+// words' adds commute -- the final value equals the 64-bit sum.
+__device__ __forceinline__ void smem_add64(unsigned long long* p, unsigned long long v) {
+  unsigned int* w = reinterpret_cast<unsigned int*>(p);
+  const unsigned int lo = (unsigned int)v, hi = (unsigned int)(v >> 32);
+  const unsigned int old = atomicAdd(w, lo);
+  const unsigned int up = hi + (unsigned int)(old + lo < old);
+  if (up) atomicAdd(w + 1, up);
+}
+
 template <int kAgg, bool kProg>
 __device__ __forceinline__ void aggregate_row(const StarParams& P, const int32_t* wstage, int row,
                                               const uint32_t (&pw)[kMaxDims], long long (&acc)[kMaxMetrics + 1],
@@ -170,7 +197,7 @@ __device__ __forceinline__ void aggregate_row(const StarParams& P, const int32_t
     if (m < nm) {
       unsigned long long v = (unsigned long long)(long long)metric_value<kProg>(P, P.metrics[m], wstage, row, pw);
       if (kAgg == AGG_DENSE_SMEM)
-        atomicAdd(s_sum + m * G + gi, v);
+        smem_add64(s_sum + m * G + gi, v);
       else
         atomicAdd(P.sums + m * G + gi, v);
     }
@@ -182,6 +209,86 @@ __device__ __forceinline__ void aggregate_row(const StarParams& P, const int32_t
     atomicAdd(P.counts + gi, 1ull);
 }
 
+// ---------------------------------------------------------------- deferred aggregation
+constexpr int kAggCap = 32;  // buffered rows per warp
+
+// An extractor over a buffered row's words (agg_src order).
+__device__ __forceinline__ uint32_t extract_entry(const Extract& x, const uint32_t* ent) {
+  if (x.dim < 0) return ent[x.slot] + (uint32_t)x.base;
+  uint32_t v = (ent[x.dim] >> x.shift) & x.mask;
+  if (x.col) v = (uint32_t)__ldg(x.col + v);
+  return v + (uint32_t)x.base;
+}
+
+template <int kAgg>
+__device__ __forceinline__ void aggregate_entry(const StarParams& P, const uint32_t* ent,
+                                                long long (&acc)[kMaxMetrics + 1], unsigned long long* s_sum,
+                                                unsigned int* s_cnt) {
+  const int nm = P.nmetrics;
+  int32_t val[kMaxMetrics];
+#pragma unroll
+  for (int m = 0; m < kMaxMetrics; m++) {
+    if (m < nm) {
+      const uint32_t a = extract_entry(P.xa_e[m], ent);
+      const int f = P.metrics[m].form;
+      uint32_t v = a;
+      if (f != MF_OPND) {
+        const uint32_t b = extract_entry(P.xb_e[m], ent);
+        v = f == MF_ADD ? a + b : f == MF_SUB ? a - b : a * b;
+      }
+      val[m] = (int32_t)v;
+    }
+  }
+  if (kAgg == AGG_SCALAR) {
+#pragma unroll
+    for (int m = 0; m < kMaxMetrics; m++)
+      if (m < nm) acc[m] += (long long)val[m];
+    acc[kMaxMetrics] += 1;
+    return;
+  }
+  const unsigned long long G = P.ngroups;
+  uint32_t gi = 0;
+  bool in_range = true;
+#pragma unroll
+  for (int q = 0; q < kMaxKeys; q++) {
+    if (q < P.nkeys) {
+      const uint32_t off = extract_entry(P.kx_e[q], ent);
+      in_range &= off < P.krange[q];
+      gi += off * (uint32_t)P.kstride[q];
+    }
+  }
+  if (!in_range) {
+    raise_error(P.error, DERR_KEY_RANGE);
+    return;
+  }
+#pragma unroll
+  for (int m = 0; m < kMaxMetrics; m++) {
+    if (m < nm) {
+      const unsigned long long v = (unsigned long long)(long long)val[m];
+      if (kAgg == AGG_DENSE_SMEM)
+        smem_add64(s_sum + m * G + gi, v);
+      else
+        atomicAdd(P.sums + m * G + gi, v);
+    }
+  }
+  if (kAgg == AGG_DENSE_SMEM)
+    s_cnt[gi] = 1u;
+  else
+    atomicAdd(P.counts + gi, 1ull);
+}
+
+// Aggregates the warp's `cnt` buffered rows, one per lane.
+template <int kAgg>
+__device__ __forceinline__ void flush_entries(const StarParams& P, const uint32_t* buf, int cnt, int lane,
+                                              long long (&acc)[kMaxMetrics + 1], unsigned long long* s_sum,
+                                              unsigned int* s_cnt) {
+  __syncwarp();
+  const int W = P.agg_words;
+  for (int base = 0; base < cnt; base += 32)
+    if (base + lane < cnt) aggregate_entry<kAgg>(P, buf + (size_t)(base + lane) * W, acc, s_sum, s_cnt);
+  __syncwarp();
+}
+
 // kFuse consecutive filter steps over the first n entries of the warp's
 // selection vector (kChunks * 32 >= n): each lane takes one entry per chunk;
 // every lookup of the fused steps is issued before any result is used (the
@@ -189,7 +296,7 @@ __device__ __forceinline__ void aggregate_row(const StarParams& P, const int32_t
 // compacted in place.  Returns the new list length.
 template <int kChunks, int kFuse>
 __device__ __forceinline__ int list_step(const Step* sts, const int32_t* wstage, const uint32_t* tables,
-                                         WarpList& L, int n, int lane, uint32_t lt) {
+                                         const WarpList& L, int n, int lane, uint32_t lt) {
   bool live[4];
   uint16_t row[4];
   uint32_t e[kFuse][4];
@@ -235,7 +342,7 @@ __device__ __forceinline__ int list_step(const Step* sts, const int32_t* wstage,
     if (st.kind == STEP_PROBE) {
 #pragma unroll
       for (int c = 0; c < kChunks; c++)
-        if (live[c]) L.pw[st.dim][row[c]] = e[f][c];
+        if (live[c]) L.pw(st.dim)[row[c]] = e[f][c];
     }
   }
   int pos[4];
@@ -255,20 +362,23 @@ __device__ __forceinline__ int list_step(const Step* sts, const int32_t* wstage,
 }
 
 template <int kAgg, bool kProg>
-__global__ void __launch_bounds__(kStarThreads, 2) star_kernel(const __grid_constant__ StarParams P) {
+__global__ void __launch_bounds__(kStarThreads, 3) star_kernel(const __grid_constant__ StarParams P) {
   extern __shared__ __align__(128) uint8_t dyn[];
   __shared__ StarSmem S;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ncols = P.ncols, nst = P.nstages;
   const size_t ring_bytes = (size_t)nst * ncols * kTileRows * 4;
   int32_t* ring = reinterpret_cast<int32_t*>(dyn);
-  WarpList* lists = reinterpret_cast<WarpList*>(dyn + ring_bytes);
-  uint32_t* tables = reinterpret_cast<uint32_t*>(lists + kConsumerWarps);
+  uint8_t* lists = dyn + ring_bytes;
+  uint32_t* tables = reinterpret_cast<uint32_t*>(lists + kConsumerWarps * warp_list_bytes(P.ndims));
   unsigned long long* s_sum =
       reinterpret_cast<unsigned long long*>(tables + ((P.smem_table_words + 3) & ~3));
   const int nm = P.nmetrics;
   const unsigned long long G = P.ngroups;
   unsigned int* s_cnt = reinterpret_cast<unsigned int*>(s_sum + (kAgg == AGG_DENSE_SMEM ? nm * G : 0));
+  // Deferred-aggregation buffers: kAggCap rows of agg_words words per consumer warp.
+  uint32_t* aggbuf = reinterpret_cast<uint32_t*>(s_cnt + (kAgg == AGG_DENSE_SMEM ? G : 0));
+  const bool deferred = !kProg && P.agg_words > 0;
 
   if (tid == 0) {
     for (int s = 0; s < nst; s++) {
@@ -318,8 +428,10 @@ __global__ void __launch_bounds__(kStarThreads, 2) star_kernel(const __grid_cons
     }
   } else {
     // ---------------- consumers
-    WarpList& L = lists[warp];
+    const WarpList L = warp_list(lists, warp, P.ndims);
     const uint32_t lt = lanemask_lt();
+    uint32_t* buf = aggbuf + (size_t)warp * kAggCap * (deferred ? P.agg_words : 0);
+    int cnt = 0;  // rows buffered (deferred aggregation)
     long long i = 0;
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
       int s = (int)(i % nst);
@@ -358,7 +470,7 @@ __global__ void __launch_bounds__(kStarThreads, 2) star_kernel(const __grid_cons
         for (int j = 0; j < 4; j++) mask |= (uint32_t)live[j] << j;
       }
       if (d0 >= 0)
-        *reinterpret_cast<uint4*>(&L.pw[d0][4 * lane]) = make_uint4(e0[0], e0[1], e0[2], e0[3]);
+        *reinterpret_cast<uint4*>(&L.pw(d0)[4 * lane]) = make_uint4(e0[0], e0[1], e0[2], e0[3]);
       int n = 0;
 #pragma unroll
       for (int j = 0; j < 4; j++) {
@@ -379,20 +491,39 @@ __global__ void __launch_bounds__(kStarThreads, 2) star_kernel(const __grid_cons
           n = list_step<4, 1>(st, wstage, tables, L, n, lane, lt);
       }
 
-      // ---- aggregate the survivors, one per lane
-      for (int base = 0; base < n; base += 32) {
-        const int idx = base + lane;
-        if (idx < n) {
+      // ---- aggregate the survivors: buffered (their operand words) and
+      // aggregated 32 rows at a time, or in place
+      if (deferred && n <= kAggCap) {
+        if (cnt + n > kAggCap) {
+          flush_entries<kAgg>(P, buf, cnt, lane, acc, s_sum, s_cnt);
+          cnt = 0;
+        }
+        const int W = P.agg_words;
+        for (int idx = lane; idx < n; idx += 32) {
           const int row = L.row[idx];
-          uint32_t pw[kMaxDims];
+          uint32_t* ent = buf + (size_t)(cnt + idx) * W;
+          for (int k = 0; k < W; k++) {
+            const int code = P.agg_src[k];
+            ent[k] = code < 8 ? L.pw(code)[row] : (uint32_t)wstage[(code - 8) * kTileRows + row];
+          }
+        }
+        cnt += n;
+      } else {
+        for (int base = 0; base < n; base += 32) {
+          const int idx = base + lane;
+          if (idx < n) {
+            const int row = L.row[idx];
+            uint32_t pw[kMaxDims];
 #pragma unroll
-          for (int d = 0; d < kMaxDims; d++) pw[d] = d < P.ndims ? L.pw[d][row] : 0u;
-          aggregate_row<kAgg, kProg>(P, wstage, row, pw, acc, s_sum, s_cnt);
+            for (int d = 0; d < kMaxDims; d++) pw[d] = d < P.ndims ? L.pw(d)[row] : 0u;
+            aggregate_row<kAgg, kProg>(P, wstage, row, pw, acc, s_sum, s_cnt);
+          }
         }
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&S.empty[s]);
     }
+    if (deferred && cnt) flush_entries<kAgg>(P, buf, cnt, lane, acc, s_sum, s_cnt);
   }
 
   if (kAgg == AGG_SCALAR) {
@@ -424,9 +555,11 @@ int star_block_size() { return kStarThreads; }
 
 size_t star_smem_bytes(const StarParams& p) {
   size_t b = (size_t)p.nstages * p.ncols * kTileRows * 4;
-  b += sizeof(WarpList) * kConsumerWarps;
+  b += warp_list_bytes(p.ndims) * kConsumerWarps;
   b += (size_t)((p.smem_table_words + 3) & ~3) * 4;
   if (p.agg == AGG_DENSE_SMEM) b += (size_t)p.ngroups * (8 * p.nmetrics + 4);
+  b = (b + 15) & ~size_t(15);
+  b += (size_t)kConsumerWarps * kAggCap * p.agg_words * 4;
   return b;
 }
 
@@ -496,7 +629,7 @@ cudaError_t launch_star(const StarParams& p, int grid, int block, size_t smem, c
 // single-query kernel, into that query's own int64 slots.
 
 __device__ __forceinline__ void batch_query_slice(const BatchQuery& Q, const BatchParams& B, const int32_t* wstage,
-                                                  long long slice_start, WarpList& L, int lane, uint32_t lt) {
+                                                  long long slice_start, const WarpList& L, int lane, uint32_t lt) {
   const long long r0 = slice_start + 4 * lane;
   uint32_t mask = 0;
 #pragma unroll
@@ -523,7 +656,7 @@ __device__ __forceinline__ void batch_query_slice(const BatchQuery& Q, const Bat
     for (int j = 0; j < 4; j++) mask |= (uint32_t)live[j] << j;
   }
   __syncwarp();
-  if (d0 >= 0) *reinterpret_cast<uint4*>(&L.pw[d0][4 * lane]) = make_uint4(e0[0], e0[1], e0[2], e0[3]);
+  if (d0 >= 0) *reinterpret_cast<uint4*>(&L.pw(d0)[4 * lane]) = make_uint4(e0[0], e0[1], e0[2], e0[3]);
   int n = 0;
 #pragma unroll
   for (int j = 0; j < 4; j++) {
@@ -552,7 +685,7 @@ __device__ __forceinline__ void batch_query_slice(const BatchQuery& Q, const Bat
     const int row = L.row[idx];
     uint32_t pw[kMaxDims];
 #pragma unroll
-    for (int d = 0; d < kMaxDims; d++) pw[d] = L.pw[d][row];
+    for (int d = 0; d < kMaxDims; d++) pw[d] = L.pw(d)[row];
     uint32_t gi = 0;
     bool in_range = true;
 #pragma unroll
@@ -602,7 +735,7 @@ __global__ void __launch_bounds__(kStarThreads, 2) batch_kernel(const __grid_con
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ncols = B.ncols, nst = B.nstages;
   int32_t* ring = reinterpret_cast<int32_t*>(dyn);
-  WarpList* lists = reinterpret_cast<WarpList*>(dyn + (size_t)nst * ncols * kTileRows * 4);
+  uint8_t* lists = dyn + (size_t)nst * ncols * kTileRows * 4;
   if (tid == 0) {
     for (int s = 0; s < nst; s++) {
       mbar_init(&full[s], 1);
@@ -646,7 +779,7 @@ __global__ void __launch_bounds__(kStarThreads, 2) batch_kernel(const __grid_con
     }
     return;
   }
-  WarpList& L = lists[warp];
+  const WarpList L = warp_list(lists, warp, kMaxDims);
   const uint32_t lt = lanemask_lt();
   for (long long i = 0;; i++) {
     const int s = (int)(i % nst);
@@ -678,7 +811,7 @@ __global__ void __launch_bounds__(kStarThreads, 2) batch_kernel(const __grid_con
 }
 
 size_t batch_smem_bytes(const BatchParams& b) {
-  return (size_t)b.nstages * b.ncols * kTileRows * 4 + sizeof(WarpList) * kConsumerWarps;
+  return (size_t)b.nstages * b.ncols * kTileRows * 4 + warp_list_bytes(kMaxDims) * kConsumerWarps;
 }
 
 int batch_grid_size(const BatchParams& b, size_t smem) {

@@ -163,6 +163,12 @@ struct StarParams {
   unsigned long long* hkeys;        // AGG_HASH_GLOBAL: packed keys per slot (~0 = empty)
   int smem_table_words;             // words of dimension tables staged in shared memory
   int* error;                       // device error word (division by zero, hash overflow)
+  // Deferred aggregation (plans without bytecode): a surviving row's operand
+  // words -- the probe words and fact values its keys and metrics read -- are
+  // appended to a per-warp buffer and aggregated 32 rows at a time.
+  int agg_words;                    // words per buffered row; 0 = aggregate in place
+  int8_t agg_src[kMaxDims + kMaxSteps];  // word k: probe word of dim d (0..3), or fact slot 8 + s
+  Extract kx_e[kMaxKeys], xa_e[kMaxMetrics], xb_e[kMaxMetrics];  // the extractors over those words
 };
 
 // ---------------------------------------------------------------- batched star queries
@@ -316,11 +322,35 @@ inline void flatten_plan(StarParams& P) {
   // measured slower (5.2 vs 4.2 ms): the second probe then runs for every row
   // the first would have removed.  The planner leaves fuse_next at 0.
   for (int q = 0; q < P.nkeys; q++) P.kx[q] = make_extract(P, P.keys[q], (int32_t)(0u - (uint32_t)P.kmin[q]));
+  bool prog = P.npost > 0;
   for (int m = 0; m < P.nmetrics; m++) {
     Metric& M = P.metrics[m];
-    if (M.form == MF_PROG) continue;
+    if (M.form == MF_PROG) {
+      prog = true;
+      continue;
+    }
     M.xa = make_extract(P, M.a, 0);
     if (M.form != MF_OPND) M.xb = make_extract(P, M.b, 0);
+  }
+  // The buffered row's words: each distinct dim or fact slot an extractor reads.
+  P.agg_words = 0;
+  if (prog) return;
+  auto word_of = [&](Extract x) {
+    const int8_t code = (int8_t)(x.dim >= 0 ? x.dim : 8 + x.slot);
+    int k = 0;
+    while (k < P.agg_words && P.agg_src[k] != code) k++;
+    if (k == P.agg_words) P.agg_src[P.agg_words++] = code;
+    if (x.dim >= 0)
+      x.dim = k;
+    else
+      x.slot = k;
+    return x;
+  };
+  for (int q = 0; q < P.nkeys; q++) P.kx_e[q] = word_of(P.kx[q]);
+  for (int m = 0; m < P.nmetrics; m++) {
+    const Metric& M = P.metrics[m];
+    P.xa_e[m] = word_of(M.xa);
+    if (M.form != MF_OPND) P.xb_e[m] = word_of(M.xb);
   }
 }
 
