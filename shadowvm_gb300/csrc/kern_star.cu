@@ -446,31 +446,30 @@ __global__ void __launch_bounds__(kStarThreads, 3) star_kernel(const __grid_cons
       if (r0 < P.row_begin) mask &= (0xFu << (unsigned)(P.row_begin - r0 > 4 ? 4 : P.row_begin - r0)) & 0xFu;
       if (r0 + 4 > P.row_end) mask &= r0 >= P.row_end ? 0u : 0xFu >> (unsigned)(r0 + 4 - P.row_end);
 
-      // ---- dense first step over the warp's 128 rows
-      uint32_t e0[4] = {0u, 0u, 0u, 0u};
-      int d0 = -1;
-      if (P.nsteps > 0) {
-        const Step& st = P.steps[0];
+      // ---- every filter step over the lane's 4 rows, predicated on the rows
+      // still live: a probe's loads go out only for live rows, its entries
+      // are kept per row in shared memory; the warp stops once no row lives.
+      for (int k = 0; k < P.nsteps; k++) {
+        if (!__any_sync(0xffffffffu, mask)) break;
+        const Step& st = P.steps[k];
         const int4 v = reinterpret_cast<const int4*>(wstage + st.col * kTileRows)[lane];
         const int32_t key[4] = {v.x, v.y, v.z, v.w};
         const uint32_t span = (uint32_t)st.hi - (uint32_t)st.lo;
         bool live[4];
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-          live[j] = (mask >> j & 1u) && (uint32_t)key[j] - (uint32_t)st.lo <= span;
-        }
+        for (int j = 0; j < 4; j++) live[j] = (mask >> j & 1u) && (uint32_t)key[j] - (uint32_t)st.lo <= span;
         if (st.kind == STEP_PROBE) {
-          d0 = st.dim;
-          lookup4(st, tables, key, live, e0);
+          uint32_t e[4];
+          lookup4(st, tables, key, live, e);
 #pragma unroll
-          for (int j = 0; j < 4; j++) live[j] = live[j] && (e0[j] & 1u);
+          for (int j = 0; j < 4; j++) live[j] = live[j] && (e[j] & 1u);
+          *reinterpret_cast<uint4*>(&L.pw(st.dim)[4 * lane]) = make_uint4(e[0], e[1], e[2], e[3]);
         }
         mask = 0;
 #pragma unroll
         for (int j = 0; j < 4; j++) mask |= (uint32_t)live[j] << j;
       }
-      if (d0 >= 0)
-        *reinterpret_cast<uint4*>(&L.pw(d0)[4 * lane]) = make_uint4(e0[0], e0[1], e0[2], e0[3]);
+      // ---- the survivors as a selection list
       int n = 0;
 #pragma unroll
       for (int j = 0; j < 4; j++) {
@@ -479,17 +478,6 @@ __global__ void __launch_bounds__(kStarThreads, 3) star_kernel(const __grid_cons
         n += __popc(b);
       }
       __syncwarp();
-
-      // ---- later steps over the selection vector (all lanes busy)
-      for (int k = 1; k < P.nsteps && n > 0; k++) {
-        const Step* st = &P.steps[k];
-        if (n <= 32)
-          n = list_step<1, 1>(st, wstage, tables, L, n, lane, lt);
-        else if (n <= 64)
-          n = list_step<2, 1>(st, wstage, tables, L, n, lane, lt);
-        else
-          n = list_step<4, 1>(st, wstage, tables, L, n, lane, lt);
-      }
 
       // ---- aggregate the survivors: buffered (their operand words) and
       // aggregated 32 rows at a time, or in place

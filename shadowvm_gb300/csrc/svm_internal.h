@@ -317,10 +317,11 @@ inline void flatten_plan(StarParams& P) {
     st.span = D.span;
     st.entry_bits = D.entry_bits;
   }
-  // The kernel can evaluate two consecutive steps in one pass (fuse_next).
-  // Pairing the two global-table probes of the 600 M-row star query that way
-  // measured slower (5.2 vs 4.2 ms): the second probe then runs for every row
-  // the first would have removed.  The planner leaves fuse_next at 0.
+  // Issuing two consecutive global-table probes together (one round trip
+  // instead of two) measured slower on the 600 M-row star query, both over
+  // selection vectors (5.2 vs 4.2 ms) and predicated per row (5.05 vs 4.67
+  // ms): the second probe then runs for every row the first would have
+  // removed.  Steps run one after another; fuse_next stays 0.
   for (int q = 0; q < P.nkeys; q++) P.kx[q] = make_extract(P, P.keys[q], (int32_t)(0u - (uint32_t)P.kmin[q]));
   bool prog = P.npost > 0;
   for (int m = 0; m < P.nmetrics; m++) {
