@@ -39,6 +39,14 @@ __device__ __forceinline__ uint32_t lane_lt() {
 }
 
 constexpr int kChunks = kTileRows / 32;     // bitmap words per tile
+// Merged words are stored by swizzled row position: row r at slot
+// (r % 32) * 32 + ((r / 32) ^ (r % 32)) of a group's region.  The 32 rows a
+// lane owns (lane L: rows L, L + 32, ..., L + 992) then sit in one 32-slot
+// block, so one transpose of a block yields a lane's bitmap words directly,
+// and both the fill (consecutive rows) and the transpose (one block) touch
+// 32 distinct banks.
+constexpr int kSlots = kTileRows;           // slots per group region (row-major words)
+__device__ __forceinline__ int row_slot(int r) { return ((r & 31) << 5) | ((r >> 5) ^ (r & 31)); }
 constexpr int kBmStride = kChunks + 1;      // a table's bitmap row, padded (conflict-free stores)
 static_assert(sizeof(MQuery) == 240 && sizeof(MExtract) == 12, "descriptor layout");
 constexpr int kDenseRows = 256;             // live rows above which a range test runs on every row
@@ -47,12 +55,12 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 // A value for the aggregation: a staged fact value, or a payload field of a
 // merged probe word (optionally a row index into a gather column), plus
-// `base`.  A group's merged words sit row-major: word w of row r at
-// group_first_word * kTileRows + r * words + w.
+// `base`.  Word w of row r of a group sits at
+// group_first_word * kSlots + row_slot(r) * words + w.
 __device__ __forceinline__ uint32_t mx(const MExtract& x, const BatchParams& B, const int32_t* stage,
                                        const uint32_t* mw, int row) {
   if (x.src < 0) return (uint32_t)stage[x.slot * kTileRows + row] + (uint32_t)x.base;
-  uint32_t v = (mw[x.src * kTileRows + row * (x.sg & 15) + x.slot] >> x.shift) & x.mask;
+  uint32_t v = (mw[x.src * kSlots + row_slot(row) * (x.sg & 15) + x.slot] >> x.shift) & x.mask;
   if (x.sg >> 4) v = (uint32_t)__ldg(B.gcol[(x.sg >> 4) - 1] + v);
   return v + (uint32_t)x.base;
 }
@@ -104,7 +112,7 @@ __device__ __forceinline__ void fill_issue(const ProbeGroup& G, const int32_t* s
   const bool in = off < G.span;
   const int W = G.words;
   const uint32_t* src = G.table + (size_t)(in ? off : 0u) * W;
-  uint32_t* dst = mwb + G.word_off * kTileRows + row * W;
+  uint32_t* dst = mwb + G.word_off * kSlots + row_slot(row) * W;
   if ((W & 3) == 0) {
     for (int h = 0; h < W; h += 4) cp_async_zfill<16>(dst + h, src + h, in, pol);
   } else if ((W & 1) == 0) {
@@ -135,12 +143,14 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
 }
 
 // One query over one staged tile (local rows [lo, hi)).  Lane L owns rows
-// [32 L, 32 L + 32) as the bits of one mask word.
+// L + 32 i (i = 0..31) as bit i of one mask word, so every per-row shared
+// memory read of a lane hits its own bank.
 __device__ __forceinline__ void mquery_tile(const MQuery& Q, const BatchParams& B, const int32_t* stage,
                                             const uint32_t* mw, const uint32_t* bm, int lo, int hi, int lane) {
-  const int r0 = 32 * lane;
-  const int a = lo - r0 > 0 ? lo - r0 : 0, b = hi - r0 < 32 ? hi - r0 : 32;
-  uint32_t m = a >= b ? 0u : (b - a == 32 ? 0xFFFFFFFFu : ((1u << (b - a)) - 1u) << a);
+  // bits i with lo <= L + 32 i < hi
+  const int ia = lo > lane ? (lo - lane + 31) >> 5 : 0;
+  const int ib = hi > lane ? ((hi - 1 - lane) >> 5) + 1 : 0;  // exclusive
+  uint32_t m = ia >= ib ? 0u : (ib - ia == 32 ? 0xFFFFFFFFu : ((1u << (ib - ia)) - 1u) << ia);
   const int np = Q.nprobe, nr = Q.nrange;
   for (int p = 0; p < np; p++) m &= bm[Q.probe_tab[p] * kBmStride + lane];
   for (int r = 0; r < nr; r++) {
@@ -152,15 +162,12 @@ __device__ __forceinline__ void mquery_tile(const MQuery& Q, const BatchParams& 
     if (live > kDenseRows) {
       uint32_t keep = 0;
 #pragma unroll 8
-      for (int i = 0; i < kChunks; i++) {
-        const uint32_t bb = __ballot_sync(0xffffffffu, (uint32_t)cv[32 * i + lane] - rlo <= span);
-        keep = lane == i ? bb : keep;
-      }
+      for (int i = 0; i < kChunks; i++) keep |= (uint32_t)((uint32_t)cv[32 * i + lane] - rlo <= span) << i;
       m &= keep;
     } else {
       for (uint32_t bb = m; bb; bb &= bb - 1) {
         const int j = __ffs(bb) - 1;
-        if ((uint32_t)cv[r0 + j] - rlo > span) m &= ~(1u << j);
+        if ((uint32_t)cv[32 * j + lane] - rlo > span) m &= ~(1u << j);
       }
     }
   }
@@ -183,7 +190,7 @@ __device__ __forceinline__ void mquery_tile(const MQuery& Q, const BatchParams& 
   const uint8_t* mf = Q.mform;
   long long acc[kMaxMetrics] = {0, 0, 0};
   for (uint32_t bb = m; bb; bb &= bb - 1) {
-    const int row = r0 + __ffs(bb) - 1;
+    const int row = 32 * (__ffs(bb) - 1) + lane;
     uint32_t gi = 0;
     bool in_range = true;
 #pragma unroll
@@ -255,10 +262,11 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
   __shared__ uint64_t fill_full[2], fill_empty[2];
   __shared__ long long stage_tile[kStages];
   __shared__ long long s_tile;
-  __shared__ int s_next;
+  __shared__ int s_next, s_na;
+  __shared__ uint32_t s_need;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ncols = B.ncols, nst = B.nstages, nq = B.nqueries;
-  const size_t mw_words = (size_t)B.nmwords * kTileRows;
+  const size_t mw_words = (size_t)B.nmwords * kSlots;
   int32_t* ring = reinterpret_cast<int32_t*>(dyn);
   uint32_t* mwbuf = reinterpret_cast<uint32_t*>(dyn + (size_t)nst * ncols * kTileRows * 4);  // two buffers
   uint32_t* bm = mwbuf + 2 * mw_words;
@@ -362,10 +370,24 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
   for (long long i = 0;; i++) {
     const int s = (int)(i % nst), b = (int)(i & 1);
     const uint32_t sp = (uint32_t)((i / nst) & 1), bp = (uint32_t)((i / 2) & 1);
-    if (tid == 0) {
-      const bool good = mbar_wait_bounded(&fill_full[b], bp, kPolls) && mbar_wait_bounded(&full[s], sp, kPolls);
-      s_tile = good ? stage_tile[s] : -2;
-      s_next = 0;
+    // Warp 0 waits for the tile, lists its queries and the probe groups they
+    // need; the other warps take the list from shared memory.
+    if (warp == 0) {
+      long long t0 = -2;
+      if (lane == 0) {
+        const bool good = mbar_wait_bounded(&fill_full[b], bp, kPolls) && mbar_wait_bounded(&full[s], sp, kPolls);
+        t0 = good ? stage_tile[s] : -2;
+        s_next = 0;
+      }
+      t0 = __shfl_sync(0xffffffffu, t0, 0);
+      int na0 = 0;
+      uint32_t need0 = 0;
+      if (t0 >= 0) need0 = tile_queries(qlo, qhi, qg, nq, a0 + t0 * kTileRows, act, true, lane, lt, &na0);
+      if (lane == 0) {
+        s_tile = t0;
+        s_na = na0;
+        s_need = need0;
+      }
     }
     consumer_bar();
     const long long t = s_tile;
@@ -380,8 +402,8 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
     const int32_t* stage = ring + (size_t)s * ncols * kTileRows;
     const uint32_t* mw = mwbuf + (size_t)b * mw_words;
     const long long tile_start = a0 + t * kTileRows, tile_end = tile_start + kTileRows;
-    int na;
-    const uint32_t need = tile_queries(qlo, qhi, qg, nq, tile_start, act, warp == 0, lane, lt, &na);
+    const int na = s_na;
+    const uint32_t need = s_need;
     // Each needed table's present bits as a row bitmap: word 0 of each row's
     // entry, transposed per 32 rows.
     const int ng = __popc(need);
@@ -391,8 +413,9 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
       for (int z = 0; z < gsel; z++) mm &= mm - 1;
       const int g = __ffs(mm) - 1;
       const ProbeGroup& G = B.probe[g];
-      const uint32_t present =
-          transpose32(mw[G.word_off * kTileRows + (chunk * 32 + lane) * G.words], lane);
+      // column `chunk` = the rows chunk + 32 i a lane owns: lane i reads row
+      // chunk + 32 i; after the transpose lane t holds table t's word.
+      const uint32_t present = transpose32(mw[G.word_off * kSlots + row_slot(chunk + 32 * lane) * G.words], lane);
       const int t0 = B.gtab0[g];
       if (lane < B.gtab0[g + 1] - t0) bm[(t0 + lane) * kBmStride + chunk] = present;
     }
@@ -449,7 +472,7 @@ cudaError_t launch_merge_build(const MergeBuild& m, uint32_t* out, cudaStream_t 
 }
 
 size_t mbatch_smem_bytes(const BatchParams& b) {
-  return (size_t)b.nstages * b.ncols * kTileRows * 4 + 2 * (size_t)b.nmwords * kTileRows * 4 +
+  return (size_t)b.nstages * b.ncols * kTileRows * 4 + 2 * (size_t)b.nmwords * kSlots * 4 +
          (size_t)kMaxMergedTables * kBmStride * 4 + (size_t)b.nqueries * (sizeof(MQuery) + 8 + 8 + 4 + 2) + 16;
 }
 
