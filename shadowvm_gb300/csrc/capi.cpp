@@ -90,6 +90,39 @@ svm_status Ctx::alloc(size_t bytes, DevBufPtr* out, bool zero) {
   return SVM_OK;
 }
 
+svm_status Ctx::upload(void* dst, const void* src, size_t bytes) {
+  constexpr size_t kPiece = size_t(64) << 20;
+  cudaError_t e;
+  if (bytes < kPiece) {
+    e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream);
+    return e ? cuda_fail(e, "cudaMemcpyAsync") : SVM_OK;
+  }
+  if (!copy_stream[0]) {
+    for (int i = 0; i < kCopyStreams; i++) {
+      if ((e = cudaStreamCreateWithFlags(&copy_stream[i], cudaStreamNonBlocking))) return cuda_fail(e, "copy stream");
+    }
+    for (int i = 0; i <= kCopyStreams; i++)
+      if ((e = cudaEventCreateWithFlags(&copy_event[i], cudaEventDisableTiming))) return cuda_fail(e, "copy event");
+  }
+  // copy streams wait for the work already on `stream` ...
+  if ((e = cudaEventRecord(copy_event[kCopyStreams], stream))) return cuda_fail(e, "cudaEventRecord");
+  for (int i = 0; i < kCopyStreams; i++)
+    if ((e = cudaStreamWaitEvent(copy_stream[i], copy_event[kCopyStreams], 0))) return cuda_fail(e, "wait");
+  size_t off = 0;
+  for (int piece = 0; off < bytes; piece++, off += kPiece) {
+    const size_t n = bytes - off < kPiece ? bytes - off : kPiece;
+    e = cudaMemcpyAsync((char*)dst + off, (const char*)src + off, n, cudaMemcpyHostToDevice,
+                        copy_stream[piece % kCopyStreams]);
+    if (e) return cuda_fail(e, "cudaMemcpyAsync");
+  }
+  // ... and `stream` waits for every piece.
+  for (int i = 0; i < kCopyStreams; i++) {
+    if ((e = cudaEventRecord(copy_event[i], copy_stream[i]))) return cuda_fail(e, "cudaEventRecord");
+    if ((e = cudaStreamWaitEvent(stream, copy_event[i], 0))) return cuda_fail(e, "wait");
+  }
+  return SVM_OK;
+}
+
 svm_status Ctx::pinned_reserve(size_t bytes) {
   if (pinned_bytes >= bytes) return SVM_OK;
   if (pinned) cudaFreeHost(pinned);
@@ -250,6 +283,10 @@ void svm_destroy(svm_ctx* c) {
   x->scratch.reset();
   x->trim_pool(0);
   if (x->pinned) cudaFreeHost(x->pinned);
+  for (int i = 0; i < svm::Ctx::kCopyStreams; i++)
+    if (x->copy_stream[i]) cudaStreamDestroy(x->copy_stream[i]);
+  for (int i = 0; i <= svm::Ctx::kCopyStreams; i++)
+    if (x->copy_event[i]) cudaEventDestroy(x->copy_event[i]);
   for (auto e : x->event_pool) cudaEventDestroy(e);
   if (x->d_error) cudaFree(x->d_error);
   if (x->stream) cudaStreamDestroy(x->stream);
@@ -299,10 +336,13 @@ svm_status svm_object_put(svm_ctx* c, const char* id, int ncols, const int* type
       if (st) return st;
     }
     if (columns && columns[k] && nrows) {
-      cudaError_t e = cudaMemcpyAsync(b->p, columns[k], nrows * el,
-                                      on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                                      x->stream);
-      if (e) return x->cuda_fail(e, "cudaMemcpyAsync");
+      if (on_device) {
+        cudaError_t e = cudaMemcpyAsync(b->p, columns[k], nrows * el, cudaMemcpyDeviceToDevice, x->stream);
+        if (e) return x->cuda_fail(e, "cudaMemcpyAsync");
+      } else {
+        svm_status st = x->upload(b->p, columns[k], nrows * el);
+        if (st) return st;
+      }
     }
     o->storage.push_back(b);
   }

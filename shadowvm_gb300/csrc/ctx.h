@@ -98,6 +98,10 @@ struct Ctx {
   // Pinned host staging for bulk reads (grows, kept).
   void* pinned = nullptr;
   size_t pinned_bytes = 0;
+  // Copy streams for large host-to-device uploads (created on first use).
+  static constexpr int kCopyStreams = 4;
+  cudaStream_t copy_stream[kCopyStreams] = {};
+  cudaEvent_t copy_event[kCopyStreams + 1] = {};
   unsigned long long next_version = 1;
   std::map<std::string, ObjectPtr> objects;
   std::map<std::string, DimTablePtr> dim_cache;
@@ -124,6 +128,10 @@ struct Ctx {
   svm_status alloc(size_t bytes, DevBufPtr* out, bool zero = false);
   void release(void* p, size_t bytes);        // a DevBuf's block: back to the pool or freed
   svm_status pinned_reserve(size_t bytes);
+  // Enqueues a host-to-device copy ordered after earlier work on `stream`
+  // and before later work on it; copies of 64 MB and more go in pieces over
+  // the copy streams so that several copy engines work at once.
+  svm_status upload(void* dst, const void* src, size_t bytes);
   void trim_pool(size_t keep);                // frees pooled blocks until at most `keep` bytes stay
   // Scratch: reset() then take() pieces; valid until the next reset().
   void scratch_reset() { scratch_used = 0; }
