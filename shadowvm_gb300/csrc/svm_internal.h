@@ -185,7 +185,7 @@ constexpr int kMaxBatchCols = 12;
 // group then serves every query of the batch that probes any of those tables.
 constexpr int kMaxProbeGroups = 8;
 constexpr int kMaxMergedWords = 16;   // merged words per row over all groups
-constexpr int kMBatchWarps = 16;      // consumer warps of the merged batch kernel
+constexpr int kMBatchWarps = 28;      // consumer warps of the merged batch kernel
 
 struct ProbeGroup {
   int col;                  // union fact column slot of the key
