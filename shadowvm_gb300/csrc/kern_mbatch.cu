@@ -451,10 +451,10 @@ __global__ void merge_build_kernel(const __grid_constant__ MergeBuild M, uint32_
       uint32_t e = S.words[bit >> 5] >> (bit & 31);
       if (S.entry_bits < 32) e &= (1u << S.entry_bits) - 1u;
       w[0] |= (e & 1u) << S.present_bit;
-      const uint32_t pay = e >> 1;
+      const uint32_t pay = S.pay_bits >= 32 ? e >> 1 : (e >> 1) & ((1u << S.pay_bits) - 1u);
 #pragma unroll
       for (int z = 0; z < 8; z++)
-        if (z == S.pay_word && S.entry_bits > 1) w[z] |= pay << S.pay_bit;
+        if (z == S.pay_word && S.pay_bits > 0) w[z] |= pay << S.pay_bit;
     }
     for (int z = 0; z < M.words; z++) out[k * M.words + z] = w[z];
   }

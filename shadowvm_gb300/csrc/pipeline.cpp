@@ -953,7 +953,11 @@ void plan_merge(const std::vector<BatchQuery>& qs, const std::vector<BatchItem>&
       long long kmin = LLONG_MAX, kmax = LLONG_MIN;
       while (next < tabs.size() && ntab < reserve) {
         const DimTablePtr& T = tabs[next];
-        const int pb = T->desc.entry_bits - 1;
+        // The payload's used width: fields sit from bit 1 up to the highest
+        // field's end (the entry's padding up to entry_bits is not carried).
+        int pb = 0;
+        for (int f = 0; f < T->desc.npay; f++)
+          pb = std::max(pb, (int)T->desc.pay[f].shift + (int)T->desc.pay[f].bits - 1);
         const long long tmin = T->desc.key_min, tmax = (long long)T->desc.key_min + T->desc.span - 1;
         const long long nmin = std::min(kmin, tmin), nmax = std::max(kmax, tmax);
         if ((nmax - nmin + 1) * 32ll > (1ll << 30)) break;
@@ -1053,8 +1057,10 @@ svm_status merged_table(Ctx* x, MergePlan* mp, int g) {
       for (size_t i = b0; i < mp->members[g].size() && mb.nsrc < kMaxMergeSrcs; i++) {
         const auto& m = mp->members[g][i];
         const DimDesc& d = m.first->desc;
-        mb.src[mb.nsrc++] =
-            MergeSrc{d.words, d.key_min, d.span, d.entry_bits, m.second.present_bit, m.second.pay_word, m.second.pay_bit};
+        int pb = 0;
+        for (int f = 0; f < d.npay; f++) pb = std::max(pb, (int)d.pay[f].shift + (int)d.pay[f].bits - 1);
+        mb.src[mb.nsrc++] = MergeSrc{d.words,   d.key_min, d.span, d.entry_bits, m.second.present_bit,
+                                     m.second.pay_word, m.second.pay_bit, pb};
         mt.srcs.push_back(m.first);
       }
       if (b0 > 0) return x->fail(SVM_E_UNSUPPORTED, "more than 32 tables in one merged probe group");

@@ -202,7 +202,8 @@ struct MergeSrc {           // one dense table placed into a merged table
   uint32_t span;
   int entry_bits;
   int present_bit;          // in word 0
-  int pay_word, pay_bit;    // the entry's payload (entry >> 1, entry_bits - 1 bits)
+  int pay_word, pay_bit;    // the entry's payload (entry >> 1) ...
+  int pay_bits;             // ... of this many bits (0: none)
 };
 
 constexpr int kMaxMergeSrcs = 32;
