@@ -875,11 +875,13 @@ struct BatchItem {
 };
 
 // Cost model of a fold, in picoseconds, measured on GB300 with the 256-query
-// star-schema mix over a 600 M-row table: one query alone costs about 5.8 ps
+// star-schema mix over a 600 M-row table: one query alone costs about 5.4 ps
 // per row it reads plus ~30 us of launch, finalize and result handling; the
-// batched launch costs about 17.7 ps per row of the union of the queries'
-// ranges (the shared scan, lookups and per-tile work) plus 1.5 ps per query
-// row, plus ~100 us.  The cheaper way runs.
+// batched launch costs about 50 ps per row of the union of the queries'
+// ranges (the shared scan, merged-table lookups, bitmaps and per-tile
+// bookkeeping: 30.1 ms for the 600 M-row union with the query work removed)
+// plus 0.39 ps per query row (9.9 ms for the mix's 25.5 G query-rows), plus
+// ~100 us.  The cheaper way runs.
 bool batch_is_cheaper(const std::vector<BatchItem>& items) {
   std::vector<std::pair<long long, long long>> iv;
   double single = 0, rows = 0;
@@ -887,7 +889,7 @@ bool batch_is_cheaper(const std::vector<BatchItem>& items) {
     const long long b = it.plan.P.row_begin, e = it.plan.empty_filter ? b : it.plan.P.row_end;
     iv.push_back({b, e});
     rows += (double)(e - b);
-    single += 5.8 * (double)(e - b) + 30e6;
+    single += 5.4 * (double)(e - b) + 30e6;
   }
   std::sort(iv.begin(), iv.end());
   double uni = 0;
@@ -902,7 +904,7 @@ bool batch_is_cheaper(const std::vector<BatchItem>& items) {
     }
   }
   if (ce > cb) uni += (double)(ce - cb);
-  const double batch = 17.7 * uni + 1.5 * rows + 100e6;
+  const double batch = 50.0 * uni + 0.39 * rows + 100e6;
   return batch < single;
 }
 
