@@ -22,6 +22,7 @@
  *                                 id like ShadowVMService::cached_obj (service/service.hpp:92)
  *   svm_run_batch                 no counterpart: many RunPipelineCMD calls folded into one launch
  *   svm_pipeline_footprint        no counterpart: device bytes a pipeline needs (served admission)
+ *   svm_object_load_text          Loader::Host (core/operator.cpp:24-48): delimited text -> columns
  */
 #ifndef SVM_CAPI_H_
 #define SVM_CAPI_H_
@@ -122,6 +123,21 @@ svm_status svm_object_read(svm_ctx* ctx, const char* id, int col, unsigned long 
                            unsigned long long n, void* host_out);
 /* Device address of column `col` (valid until the object is dropped/replaced). */
 svm_status svm_object_device_ptr(svm_ctx* ctx, const char* id, int col, void** dptr);
+/* Parses delimited text into a new object, on the device: the reference's
+ * Loader operator (Loader::Host, core/operator.cpp:24-48, items converted by
+ * GetValueOfItemBySwitch, com/cpp/com.cu:33-44), e.g. SSB's "a|b|c|\n"
+ * lines with col_delim '|' and row_delim '\n'.  A field is stored when a
+ * column delimiter ends it (the text after a line's last column delimiter is
+ * dropped); rows are counted by row delimiters; Int32 fields convert as
+ * atoi, Int64 as atol (strtol, clamped on overflow).  Fields past column
+ * ncols - 1 are ignored and columns a row does not reach are 0 (the
+ * reference leaves both undefined).  Columns must be SVM_INT32 or
+ * SVM_INT64; an item longer than 4095 bytes is SVM_E_INVALID_ARG.  `text`
+ * is host memory, or device memory with on_device = 1. */
+svm_status svm_object_load_text(svm_ctx* ctx, const char* id, int ncols, const int* types, const char* text,
+                                unsigned long long bytes, int on_device, char col_delim, char row_delim,
+                                unsigned long long* nrows_out);
+
 /* Several whole objects to host memory in one device pass (one gather kernel,
  * one copy, one synchronisation).  For each object in order and each of its
  * columns in order, the column's rows are written to `host` starting at an

@@ -63,6 +63,36 @@ def build_port() -> str:
     return out
 
 
+def build_loader() -> str:
+    """Compile the Loader restatement (loader.c); returns the library path."""
+    os.makedirs(BUILD, exist_ok=True)
+    out = os.path.join(BUILD, "libsvm_oracle_loader.so")
+    src = os.path.join(HERE, "loader.c")
+    if not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
+        _run(["gcc", "-O2", "-fPIC", "-shared", src, "-o", out + ".tmp"])
+        os.replace(out + ".tmp", out)
+    return out
+
+
+def load_text(text: bytes, types: list, col_delim: str = "|", row_delim: str = "\n", cap_rows: int | None = None):
+    """The reference Loader over `text` (restated in loader.c): returns
+    (rows, [column arrays]); raises ValueError for an item over 4095 bytes."""
+    lib = ctypes.CDLL(build_loader())
+    f = lib.svm_oracle_load_text
+    f.restype = ctypes.c_longlong
+    f.argtypes = [ctypes.c_char_p, ctypes.c_ulonglong, ctypes.c_char, ctypes.c_char, ctypes.c_int,
+                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_void_p), ctypes.c_ulonglong]
+    if cap_rows is None:
+        cap_rows = text.count(row_delim.encode())
+    cols = [np.zeros(cap_rows + 1, np.int64 if int(t) == 3 else np.int32) for t in types]
+    ptrs = (ctypes.c_void_p * len(cols))(*[c.ctypes.data for c in cols])
+    tt = (ctypes.c_int * len(types))(*[int(t) for t in types])
+    n = f(text, len(text), col_delim.encode(), row_delim.encode(), len(types), tt, ptrs, cap_rows)
+    if n < 0:
+        raise ValueError("an item longer than 4095 bytes")
+    return n, [c[:min(n, cap_rows)] for c in cols]
+
+
 def ref_available() -> bool:
     return os.path.exists(os.path.join(REF, "libsvm_oracle_ref.so")) and \
         os.path.exists(os.path.join(REF, "ref_codegen"))

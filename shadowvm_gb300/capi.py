@@ -104,6 +104,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "svm_object_read": (I, [P, cp, I, U64, U64, P]),
         "svm_object_device_ptr": (I, [P, cp, I, ctypes.POINTER(P)]),
         "svm_object_drop": (I, [P, cp]),
+        "svm_object_load_text": (I, [P, cp, I, ctypes.POINTER(I), P, U64, I, ctypes.c_char, ctypes.c_char,
+                                     ctypes.POINTER(U64)]),
         "svm_objects_read": (I, [P, I, ctypes.POINTER(cp), P, U64, ctypes.POINTER(U64), ctypes.POINTER(U64)]),
         "svm_run_pipeline": (I, [P, ctypes.POINTER(svm_pipeline)]),
         "svm_run_batch": (I, [P, I, ctypes.POINTER(svm_pipeline)]),

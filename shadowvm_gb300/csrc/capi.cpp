@@ -352,6 +352,75 @@ svm_status svm_object_put(svm_ctx* c, const char* id, int ncols, const int* type
   return SVM_OK;
 }
 
+svm_status svm_object_load_text(svm_ctx* c, const char* id, int ncols, const int* types, const char* text,
+                                unsigned long long bytes, int on_device, char col_delim, char row_delim,
+                                unsigned long long* nrows_out) {
+  if (!c || !id || ncols <= 0 || ncols > svm::kLoadMaxCols || !types || (bytes && !text)) return SVM_E_INVALID_ARG;
+  if (col_delim == row_delim) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  cudaSetDevice(x->device);
+  x->err.clear();
+  for (int k = 0; k < ncols; k++)
+    if (types[k] != SVM_INT32 && types[k] != SVM_INT64)
+      return x->fail(SVM_E_UNSUPPORTED, "text loader: columns must be Int32 or Int64 (strings are not loaded)");
+  // Host text is uploaded first; device text is read where it is.
+  svm::DevBufPtr tbuf;
+  svm_status st = SVM_OK;
+  cudaError_t e = cudaSuccess;
+  const uint8_t* dtext = (const uint8_t*)text;
+  if (!on_device && bytes) {
+    if ((st = x->alloc(bytes, &tbuf, false)) || (st = x->upload(tbuf->p, text, bytes))) return st;
+    dtext = (const uint8_t*)tbuf->p;
+  }
+  // Chunk index and the row count.
+  x->scratch_reset();
+  const size_t entries = svm::load_scratch_entries(bytes);
+  if ((st = x->scratch_reserve(entries * sizeof(svm::LoadPos) + 1024))) return st;
+  void* scr;
+  if ((st = x->scratch_take(entries * sizeof(svm::LoadPos), &scr))) return st;
+  svm::LoadPos total{0ull, 0u, 0u};
+  e = svm::launch_load_index(dtext, bytes, col_delim, row_delim, (svm::LoadPos*)scr, x->stream);
+  if (!e && bytes)
+    e = cudaMemcpyAsync(&total, svm::load_total((const svm::LoadPos*)scr, bytes), sizeof(total),
+                        cudaMemcpyDeviceToHost, x->stream);
+  if (!e) e = cudaStreamSynchronize(x->stream);
+  if (e) return x->cuda_fail(e, "text loader index");
+  // The object, every column zero until a field fills it.
+  auto o = std::make_shared<svm::Object>();
+  o->id = id;
+  o->version = x->next_version++;
+  o->ncols = ncols;
+  o->nrows = total.rows;
+  o->has_bulks = total.rows > 0;
+  o->bulk0_rows = total.rows < x->cfg.tuple_per_bulk ? total.rows : x->cfg.tuple_per_bulk;
+  o->source_rows = total.rows;
+  const unsigned long long prow = (total.rows + 63) / 64 * 64 + 64;
+  svm::LoadOut out{};
+  out.ncols = ncols;
+  out.nrows = total.rows;
+  for (int k = 0; k < ncols; k++) {
+    svm::DevBufPtr b;
+    if ((st = x->alloc(prow * (types[k] == SVM_INT64 ? 8 : 4), &b, true))) return st;
+    o->types.push_back(types[k]);
+    o->storage.push_back(b);
+    out.col[k] = b->p;
+    out.wide[k] = types[k] == SVM_INT64;
+  }
+  int zero = 0;
+  e = cudaMemcpyAsync(x->d_error, &zero, sizeof(int), cudaMemcpyHostToDevice, x->stream);
+  if (!e) e = svm::launch_load_parse(dtext, bytes, col_delim, row_delim, (const svm::LoadPos*)scr, out, x->d_error,
+                                     x->stream);
+  int h = 0;
+  if (!e) e = cudaMemcpyAsync(&h, x->d_error, sizeof(int), cudaMemcpyDeviceToHost, x->stream);
+  if (!e) e = cudaStreamSynchronize(x->stream);
+  if (e) return x->cuda_fail(e, "text loader parse");
+  if (h) return x->fail(SVM_E_INVALID_ARG, "text loader: an item longer than 4095 bytes");
+  x->objects[id] = o;
+  if (nrows_out) *nrows_out = total.rows;
+  return SVM_OK;
+}
+
 svm_status svm_object_gen_uniform(svm_ctx* c, const char* id, int col, unsigned long long seed,
                                   unsigned long long stream, unsigned long long row0, int lo, int hi,
                                   const int* lookup) {

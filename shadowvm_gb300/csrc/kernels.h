@@ -105,6 +105,29 @@ cudaError_t launch_batch_finalize(const BatchQuery* Q, int nq, const unsigned lo
                                   unsigned long long total, uint32_t* flags, unsigned long long* pos,
                                   unsigned long long* scan_tmp, const BatchOut* out, cudaStream_t s);
 
+// ---- text loader (kern_load.cu)
+struct LoadPos {                    // a chunk's rows and trailing fields (scan element)
+  unsigned long long rows;
+  unsigned int cols;
+  unsigned int has;                 // the chunk holds a row delimiter
+};
+constexpr int kLoadMaxCols = 64;
+struct LoadOut {
+  int ncols;
+  unsigned long long nrows;
+  void* col[kLoadMaxCols];
+  uint8_t wide[kLoadMaxCols];       // 1: int64 column
+};
+size_t load_chunks(unsigned long long bytes);
+size_t load_scratch_entries(unsigned long long bytes);  // LoadPos entries
+// Chunk summaries and their exclusive scan into `scratch` (text: `bytes`
+// bytes of device memory, any alignment).
+cudaError_t launch_load_index(const uint8_t* text, unsigned long long bytes, char cd, char rd, LoadPos* scratch,
+                              cudaStream_t s);
+const LoadPos* load_total(const LoadPos* scratch, unsigned long long bytes);  // rows = row delimiters
+cudaError_t launch_load_parse(const uint8_t* text, unsigned long long bytes, char cd, char rd,
+                              const LoadPos* scratch, const LoadOut& out, int* error, cudaStream_t s);
+
 // ---- merged-probe batch (kern_mbatch.cu)
 cudaError_t launch_merge_build(const MergeBuild& m, uint32_t* out, cudaStream_t s);
 size_t mbatch_smem_bytes(const BatchParams& b);

@@ -132,6 +132,22 @@ class Engine:
         nc, _ = self.info(oid)
         return [self.read(oid, c) for c in range(nc)]
 
+    def load_text(self, oid: str, text, types: list, col_delim: str = "|", row_delim: str = "\n",
+                  device_ptr: int | None = None, nbytes: int | None = None) -> int:
+        """Delimited text -> object `oid` on the device, as the reference's
+        Loader operator parses it; returns rows.  `text` is host bytes (or a
+        buffer), or pass device_ptr / nbytes for text already on the device."""
+        t = (ctypes.c_int * len(types))(*[int(x) for x in types])
+        n = ctypes.c_ulonglong()
+        if device_ptr is not None:
+            ptr, size, on_dev = ctypes.c_void_p(device_ptr), nbytes, 1
+        else:
+            buf = np.frombuffer(memoryview(text), np.uint8) if not isinstance(text, np.ndarray) else text
+            ptr, size, on_dev = buf.ctypes.data_as(ctypes.c_void_p), buf.nbytes, 0
+        self._check(self.lib.svm_object_load_text(self.h, oid.encode(), len(types), t, ptr, size, on_dev,
+                                                  col_delim.encode(), row_delim.encode(), ctypes.byref(n)))
+        return n.value
+
     def read_objects(self, oids: list[str], types: list[list[int]]) -> list[list[np.ndarray]]:
         """Whole objects in one device pass (svm_objects_read); types[k] lists
         object k's column types (ValType.Int32 / Int64)."""

@@ -293,3 +293,27 @@ def run_engine(engine, w: Workload):
         engine.run(p)
     engine.run(w.query)
     return engine.result(w.query.id, w.key_num)
+
+
+def ssb_like_text(rows: int, ncols: int, seed: int, width: int = 10) -> tuple[bytes, list]:
+    """SSB-like text for the Loader: `rows` lines of `ncols` right-aligned
+    decimals padded with spaces to `width` bytes, '|' after each field and
+    '\\n' after each line ((width + 1) * ncols + 1 bytes a line).  Returns
+    the text and the int64 columns it holds."""
+    rng = np.random.default_rng(seed)
+    vals = rng.integers(-10 ** 8, 10 ** 9, size=(rows, ncols), dtype=np.int64)
+    buf = np.full((rows, ncols, width + 1), ord(" "), np.uint8)
+    buf[:, :, width] = ord("|")
+    a = np.abs(vals)
+    for d in range(width - 1, -1, -1):
+        digit = (a % 10).astype(np.uint8) + ord("0")
+        show = (a > 0) | (d == width - 1)
+        buf[:, :, d] = np.where(show, digit, buf[:, :, d])
+        a //= 10
+    # the minus sign before the first digit
+    ndig = np.maximum(1, np.floor(np.log10(np.maximum(np.abs(vals), 1))).astype(int) + 1)
+    neg = vals < 0
+    r, c = np.nonzero(neg)
+    buf[r, c, width - 1 - ndig[r, c]] = ord("-")
+    lines = np.concatenate([buf.reshape(rows, -1), np.full((rows, 1), ord("\n"), np.uint8)], axis=1)
+    return lines.tobytes(), [vals[:, k] for k in range(ncols)]
