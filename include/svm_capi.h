@@ -262,7 +262,7 @@ svm_status svm_scan_aggregate_noalloc(svm_ctx* ctx, const svm_noalloc_scan* q, i
  * (SVM_K_*), the number of launches and the summed event time in ms since the
  * last reset. */
 enum { SVM_K_STAR = 0, SVM_K_SELECT = 1, SVM_K_BUILD = 2, SVM_K_FINALIZE = 3, SVM_K_BATCH = 4,
-       SVM_K_OTHER = 5, SVM_K_COUNT = 6 };
+       SVM_K_OTHER = 5, SVM_K_LOAD = 6 /* text Loader parse */, SVM_K_COUNT = 7 };
 svm_status svm_profile_enable(svm_ctx* ctx, int on);
 svm_status svm_profile_reset(svm_ctx* ctx);
 svm_status svm_profile_read(svm_ctx* ctx, int kernel_class, unsigned long long* launches,

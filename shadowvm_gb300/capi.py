@@ -19,7 +19,7 @@ STATUS = {0: "SVM_OK", 1: "SVM_E_INVALID_ARG", 2: "SVM_E_UNSUPPORTED", 3: "SVM_E
           4: "SVM_E_TIMEOUT", 5: "SVM_E_CUDA", 6: "SVM_E_NOT_FOUND", 7: "SVM_E_DEVICE"}
 OK, E_INVALID_ARG, E_UNSUPPORTED, E_OOM_BUDGET, E_TIMEOUT, E_CUDA, E_NOT_FOUND, E_DEVICE = range(8)
 JOIN_REF_COMPAT, JOIN_EXACT = 0, 1
-K_STAR, K_SELECT, K_BUILD, K_FINALIZE, K_BATCH, K_OTHER, K_COUNT = range(7)
+K_STAR, K_SELECT, K_BUILD, K_FINALIZE, K_BATCH, K_OTHER, K_LOAD, K_COUNT = range(8)
 
 
 class svm_config(ctypes.Structure):

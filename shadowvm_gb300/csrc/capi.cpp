@@ -373,14 +373,17 @@ svm_status svm_object_load_text(svm_ctx* c, const char* id, int ncols, const int
     if ((st = x->alloc(bytes, &tbuf, false)) || (st = x->upload(tbuf->p, text, bytes))) return st;
     dtext = (const uint8_t*)tbuf->p;
   }
-  // Chunk index and the row count.
+  // Span index and the row count.
   x->scratch_reset();
   const size_t entries = svm::load_scratch_entries(bytes);
   if ((st = x->scratch_reserve(entries * sizeof(svm::LoadPos) + 1024))) return st;
   void* scr;
   if ((st = x->scratch_take(entries * sizeof(svm::LoadPos), &scr))) return st;
   svm::LoadPos total{0ull, 0u, 0u};
+  cudaEvent_t ev;
+  x->prof_begin(SVM_K_OTHER, &ev);
   e = svm::launch_load_index(dtext, bytes, col_delim, row_delim, (svm::LoadPos*)scr, x->stream);
+  x->prof_end(SVM_K_OTHER, ev);
   if (!e && bytes)
     e = cudaMemcpyAsync(&total, svm::load_total((const svm::LoadPos*)scr, bytes), sizeof(total),
                         cudaMemcpyDeviceToHost, x->stream);
@@ -409,8 +412,12 @@ svm_status svm_object_load_text(svm_ctx* c, const char* id, int ncols, const int
   }
   int zero = 0;
   e = cudaMemcpyAsync(x->d_error, &zero, sizeof(int), cudaMemcpyHostToDevice, x->stream);
-  if (!e) e = svm::launch_load_parse(dtext, bytes, col_delim, row_delim, (const svm::LoadPos*)scr, out, x->d_error,
-                                     x->stream);
+  if (!e) {
+    x->prof_begin(SVM_K_LOAD, &ev);
+    e = svm::launch_load_parse(dtext, bytes, col_delim, row_delim, (const svm::LoadPos*)scr, out, x->d_error,
+                               x->stream);
+    x->prof_end(SVM_K_LOAD, ev);
+  }
   int h = 0;
   if (!e) e = cudaMemcpyAsync(&h, x->d_error, sizeof(int), cudaMemcpyDeviceToHost, x->stream);
   if (!e) e = cudaStreamSynchronize(x->stream);

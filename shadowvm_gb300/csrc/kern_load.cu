@@ -18,9 +18,11 @@
 // Within a span the warp walks 512-byte sub-tiles, lane l owning granule l:
 // 16-bit masks of its column and row delimiters (SWAR byte compares), one
 // packed warp scan for the row and column at the granule's start, a ballot
-// for where its first field began, then the lane converts the fields that end
-// in its granule, in warp-uniform rounds.  Field bytes are read from the span
-// staged in shared memory (plus a 64-byte halo before it).
+// for where its first field began; the lane then lists the fields that end in
+// its granule (start, end, row, column) in a per-warp list in text order.
+// Once 64 or more fields wait, the warp converts them 32 at a time, so every
+// lane has a field in every round but the last.  Field bytes are read from
+// the span staged in shared memory (plus a 64-byte halo before it).
 //
 // Items convert as strtol(s, NULL, 10) on LP64 -- leading isspace, optional
 // sign, decimal digits, clamp to the 64-bit range on overflow -- then Int32
@@ -290,12 +292,25 @@ __device__ __forceinline__ bool convert_staged(const uint8_t* p, const uint8_t* 
   return p - d0 <= 18;  // 10^18 - 1 < 2^63: no clamp
 }
 
+// A field waiting for conversion: start + 4096 (13 bits), end (12 bits) and
+// column (bits 25..31) relative to the span, and its row relative to the
+// span's first row.  kNoField fills the slot of a field that is not stored.
+constexpr int kListFlush = 64;                  // convert once this many wait
+constexpr int kListCap = kListFlush - 1 + kSub;  // plus one sub-tile's worth
+constexpr uint32_t kNoField = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t pack_field(int fs, int fe, uint32_t c) {
+  return (uint32_t)(fs + kSpan) | ((uint32_t)fe << 13) | (c << 25);
+}
+
 template <bool kFree>
 __global__ void __launch_bounds__(kWarps * 32) load_parse_kernel(const uint8_t* text, unsigned long long bytes,
                                                                 char cd, char rd, unsigned long long nspans,
                                                                 const LoadPos* pre, const LoadPos* block_tot,
                                                                 LoadOut out, int* error) {
   __shared__ __align__(16) uint8_t stage[kWarps][kStage];
+  __shared__ uint32_t list_f[kWarps][kListCap];
+  __shared__ uint32_t list_r[kWarps][kListCap];
   __shared__ void* colp[kLoadMaxCols];
   __shared__ uint8_t wide[kLoadMaxCols];
   if (threadIdx.x < kLoadMaxCols) {
@@ -307,6 +322,8 @@ __global__ void __launch_bounds__(kWarps * 32) load_parse_kernel(const uint8_t* 
   const int lane = threadIdx.x & 31;
   const uint32_t lt = (1u << lane) - 1u;  // lanes below this one
   uint8_t* st = stage[threadIdx.x >> 5];
+  uint32_t* lf = list_f[threadIdx.x >> 5];
+  uint32_t* lr = list_r[threadIdx.x >> 5];
   const uint32_t cdx = rep4(cd), rdx = rep4(rd);
   const uint32_t ncols = (uint32_t)out.ncols;
   const unsigned long long nrows = out.nrows;
@@ -325,9 +342,11 @@ __global__ void __launch_bounds__(kWarps * 32) load_parse_kernel(const uint8_t* 
     }
     __syncwarp();
     const LoadPos p0 = combine(block_tot[s / kScanBlock], pre[s]);
-    unsigned long long row = p0.rows;
+    const unsigned long long row_base = p0.rows;
+    uint32_t row = 0;  // relative to row_base
     uint32_t col = p0.cols;
     int pend = pending_start(tx, st, b0, (uint8_t)cd, (uint8_t)rd, lane);  // relative to b0
+    int nlist = 0;
 #pragma unroll 1
     for (int q = 0; q < kSpan / kSub; q++) {
       const int gbr = q * kSub + lane * 16;  // the granule's byte 0, relative to b0
@@ -355,39 +374,31 @@ __global__ void __launch_bounds__(kWarps * 32) load_parse_kernel(const uint8_t* 
       const uint32_t rbelow = rbal & lt;
       const uint32_t y_last = __shfl_sync(0xffffffffu, y, rbelow ? 31 - __clz(rbelow) : 0);
       const uint32_t c0 = rbelow ? cd_before - y_last : col + cd_before;
-      const unsigned long long r0 = row + (exc & 0xFFFFu);
+      const uint32_t r0 = row + (exc & 0xFFFFu);
       // Where the lane's first field began.
       const uint32_t dbal = __ballot_sync(0xffffffffu, dm != 0);
       const uint32_t dbelow = dbal & lt;
       const int lastpos = gbr + 31 - __clz(dm);  // meaningful when dm != 0
       const int lp = __shfl_sync(0xffffffffu, lastpos, dbelow ? 31 - __clz(dbelow) : 0);
       const int start0 = dbelow ? lp + 1 : pend;
-      // The lane's column delimiters in order, every lane in step; each
-      // field's row, column and start follow from the masks below its end.
-      uint32_t cm = cd16;
-      while (__any_sync(0xffffffffu, cm != 0)) {
-        if (cm) {
-          const int j = __ffs(cm) - 1;
-          cm &= cm - 1;
-          const uint32_t below = (1u << j) - 1u;
-          const uint32_t rb = rd16 & below, db = dm & below;
-          const unsigned long long r = r0 + __popc(rb);
-          const uint32_t c = rb ? __popc(cd16 & below & ~((2u << (31 - __clz(rb))) - 1u)) : c0 + __popc(cd16 & below);
-          const int fs = db ? gbr + 32 - __clz(db) : start0;  // the field's first byte
-          const int fe = gbr + j;                             // its column delimiter
-          if (fe - fs > kMaxItem) {                           // also an unknown start
-            raise_error(error, DERR_LOAD_ITEM);
-          } else if (c < ncols && r < nrows) {
-            const bool wd = wide[c];
-            long long val = 0;
-            if (fs < -kHalo || !convert_staged<kFree>(st + kHalo + fs, st + kHalo + fe, wd, val))
-              val = convert_global(tx, b0 + fs, b0 + fe);
-            if (wd)
-              reinterpret_cast<long long*>(colp[c])[r] = val;
-            else
-              reinterpret_cast<int32_t*>(colp[c])[r] = (int32_t)(uint32_t)(unsigned long long)val;
-          }
-        }
+      // List the lane's fields in text order; each field's row, column and
+      // start follow from the masks below its column delimiter.
+      int slot = nlist + (int)cd_before;
+      for (uint32_t cm = cd16; cm; cm &= cm - 1, slot++) {
+        const int j = __ffs(cm) - 1;
+        const uint32_t below = (1u << j) - 1u;
+        const uint32_t rb = rd16 & below, db = dm & below;
+        const uint32_t r = r0 + __popc(rb);
+        const uint32_t c = rb ? __popc(cd16 & below & ~((2u << (31 - __clz(rb))) - 1u)) : c0 + __popc(cd16 & below);
+        const int fs = db ? gbr + 32 - __clz(db) : start0;  // the field's first byte
+        const int fe = gbr + j;                             // its column delimiter
+        uint32_t f = kNoField;
+        if (fe - fs > kMaxItem)                              // also an unknown start
+          raise_error(error, DERR_LOAD_ITEM);
+        else if (c < ncols && row_base + r < nrows)
+          f = pack_field(fs, fe, c);
+        lf[slot] = f;
+        lr[slot] = r;
       }
       // Carry the row, column and pending item into the next sub-tile.
       const uint32_t tot = __shfl_sync(0xffffffffu, inc, 31);
@@ -396,6 +407,27 @@ __global__ void __launch_bounds__(kWarps * 32) load_parse_kernel(const uint8_t* 
       row += tot & 0xFFFFu;
       const int lp_end = __shfl_sync(0xffffffffu, lastpos, dbal ? 31 - __clz(dbal) : 0);
       if (dbal) pend = lp_end + 1;
+      nlist += (int)(tot >> 16);
+      if (nlist < kListFlush && q + 1 < kSpan / kSub) continue;
+      // Convert the listed fields, 32 at a time.
+      __syncwarp();
+      for (int k = lane; k < nlist; k += 32) {
+        const uint32_t f = lf[k];
+        if (f == kNoField) continue;
+        const int fs = (int)(f & 0x1FFFu) - kSpan, fe = (int)((f >> 13) & 0xFFFu);
+        const uint32_t c = f >> 25;
+        const bool wd = wide[c];
+        long long val = 0;
+        if (fs < -kHalo || !convert_staged<kFree>(st + kHalo + fs, st + kHalo + fe, wd, val))
+          val = convert_global(tx, b0 + fs, b0 + fe);
+        const unsigned long long r = row_base + lr[k];
+        if (wd)
+          reinterpret_cast<long long*>(colp[c])[r] = val;
+        else
+          reinterpret_cast<int32_t*>(colp[c])[r] = (int32_t)(uint32_t)(unsigned long long)val;
+      }
+      __syncwarp();
+      nlist = 0;
     }
   }
 }
@@ -450,13 +482,12 @@ cudaError_t launch_load_parse(const uint8_t* text, unsigned long long bytes, cha
                               const LoadPos* scratch, const LoadOut& out, int* error, cudaStream_t s) {
   const unsigned long long n = load_chunks(bytes);
   if (n == 0) return cudaSuccess;
-  // Neither delimiter a digit, sign or space: walks need no end check.
-  auto numeric = [](char ch) {
-    const uint8_t u = (uint8_t)ch;
-    return (u >= '0' && u <= '9') || u == '+' || u == '-' || u == ' ' || (u >= '\t' && u <= '\r');
-  };
+  // A field never holds a row delimiter and always ends at a column
+  // delimiter: when that is no digit, sign or space, it ends every walk.
+  const uint8_t u = (uint8_t)cd;
+  const bool numeric = (u >= '0' && u <= '9') || u == '+' || u == '-' || u == ' ' || (u >= '\t' && u <= '\r');
   note_launch();
-  if (!numeric(cd) && !numeric(rd))
+  if (!numeric)
     load_parse_kernel<true><<<grid_for(load_parse_kernel<true>, &parse_per_sm[1], n), kWarps * 32, 0, s>>>(
         text, bytes, cd, rd, n, scratch + n, scratch + 2 * n, out, error);
   else
