@@ -8,7 +8,7 @@ RunPipelineCMD of that fact pipeline (scan + probes + aggregate + result
 materialisation); the dimension pipelines and their tables are built during
 warm-up and stay cached, as in the served form.
 
-  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--config 0|1|2]
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--config 0|1|2|5]
 
 Under torchrun each rank owns its own slice of one global fact table (rows
 rank*R .. rank*R+R-1), so per-GPU work is fixed ("weak" scaling); ranks only
@@ -57,7 +57,9 @@ def committed_traffic(config: int):
     p = os.path.join(ROOT, "profiles", "star_kernel_traffic.json")
     try:
         d = json.load(open(p))
-        return d[f"config{config}"]
+        # config 5 runs config 2's kernel over the same fact columns (String
+        # dimensions only change the probe tables' payloads)
+        return d[f"config{2 if config == 5 else config}"]
     except Exception:
         return None
 
@@ -117,7 +119,7 @@ def cpu_reference_run(cfg: int, sample_rows: int, steps: int, threads: int):
     import oracle
     from shadowvm_gb300 import workloads as W
     w = W.make(cfg, fact_rows=sample_rows)
-    used = {0: [0, 1, 2, 3], 1: [0, 4, 5], 2: [0, 5, 6, 7, 8]}[cfg]
+    used = {0: [0, 1, 2, 3], 1: [0, 4, 5], 2: [0, 5, 6, 7, 8], 5: [0, 5, 6, 7, 8]}[cfg]
     fact = []
     from shadowvm_gb300 import datagen as dg
     # generate only the columns the query reads; the others stay zero
@@ -142,7 +144,7 @@ def cpu_reference_run(cfg: int, sample_rows: int, steps: int, threads: int):
 def default_cpu_sample(cfg: int, threads: int) -> int:
     """One reference bulk per host thread (the reference runs one task per bulk,
     core/pipeline.cu:161-212), at most 32 bulks."""
-    tpb = 3_000_000 if cfg == 2 else 2_000_000
+    tpb = 3_000_000 if cfg in (2, 5) else 2_000_000
     return tpb * max(4, min(threads, 32))
 
 
@@ -173,9 +175,11 @@ def reference_arm(args):
 def workload_config(cfg: int, rows: int):
     names = {0: "date join, SUM(extprice*discount)", 1: "date+part join, GROUP BY (year, brand) SUM(revenue)",
              2: "4-dimension star schema: date+customer+supplier join, GROUP BY (c_nation, s_nation, year) "
-                "SUM(revenue-supplycost)"}
+                "SUM(revenue-supplycost)",
+             5: "config 2 with String geography columns: StrCmp region filters, GROUP BY the c_nation / "
+                "s_nation strings (Hash keys) and year"}
     return {"workload": f"config {cfg}: {names[cfg]}", "fact_rows": rows,
-            "fact_columns_read": {0: 4, 1: 3, 2: 5}[cfg], "int32_columns": True,
+            "fact_columns_read": {0: 4, 1: 3, 2: 5, 5: 5}[cfg], "int32_columns": True,
             "l2": "inputs larger than L2 (no flush needed)" if rows * 4 > 129e6 else "flush not applied"}
 
 
@@ -304,7 +308,7 @@ def ours_arm(args):
     # pinned host memory every step and the result read back to the host.
     e2e = None
     if not args.no_e2e:
-        used = {0: [0, 1, 2, 3], 1: [0, 4, 5], 2: [0, 5, 6, 7, 8]}[args.config]
+        used = {0: [0, 1, 2, 3], 1: [0, 4, 5], 2: [0, 5, 6, 7, 8], 5: [0, 5, 6, 7, 8]}[args.config]
         pinned = {}
         for c in used:
             t = torch.empty(rows, dtype=torch.int32, pin_memory=True)
@@ -574,7 +578,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2, 3, 4])
+    ap.add_argument("--config", type=int, default=2, choices=[0, 1, 2, 3, 4, 5])
     ap.add_argument("--rows", type=int, default=None, help="fact rows per GPU (default: the config's)")
     ap.add_argument("--cpu-sample-rows", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")

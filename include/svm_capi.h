@@ -23,6 +23,8 @@
  *   svm_run_batch                 no counterpart: many RunPipelineCMD calls folded into one launch
  *   svm_pipeline_footprint        no counterpart: device bytes a pipeline needs (served admission)
  *   svm_object_load_text          Loader::Host (core/operator.cpp:24-48): delimited text -> columns
+ *   svm_object_put_columns        RamObject bulks with String columns (ValType String, com/svm.proto:62-72;
+ *                                 StrCmp / Hash / StrCopy of com/cpp/cpu-runtime.hpp:37-77 act on them)
  */
 #ifndef SVM_CAPI_H_
 #define SVM_CAPI_H_
@@ -95,6 +97,11 @@ void* svm_stream(svm_ctx* ctx);
 /* Device bytes currently held by the context (objects, tables, scratch). */
 unsigned long long svm_bytes_in_use(const svm_ctx* ctx);
 
+typedef struct svm_column_desc { /* ColumnInfo (svm.proto:73-79) */
+  int type;                      /* SVM_INT32, SVM_INT64, SVM_STRING ... */
+  long long val_size;
+} svm_column_desc;
+
 /* ---- object store (device-resident int32/int64 columns) ------------------ */
 /* Create object `id` with `ncols` columns of `nrows` rows each.  types[c] is
  * SVM_INT32 or SVM_INT64.  columns[c] points at nrows values in host memory
@@ -104,6 +111,16 @@ unsigned long long svm_bytes_in_use(const svm_ctx* ctx);
 svm_status svm_object_put(svm_ctx* ctx, const char* id, int ncols, const int* types,
                           unsigned long long nrows, const void* const* columns,
                           int columns_on_device);
+/* As svm_object_put, with each column described by {type, val_size}:
+ * SVM_INT32 / SVM_INT64 as above, or SVM_STRING of val_size bytes per value
+ * (the reference's fixed-width char[val_size] String column, com/svm.proto:
+ * 62-72): columns[c] points at nrows x val_size bytes.  A String column is
+ * dictionary-encoded (distinct values sorted bytewise, an int32 code per row
+ * on the device); StrCmp predicates, ReduceBy keys (the reference's
+ * Hash(value, val_size)) and Map copies work on the codes. */
+svm_status svm_object_put_columns(svm_ctx* ctx, const char* id, int ncols, const svm_column_desc* cols,
+                                  unsigned long long nrows, const void* const* columns,
+                                  int columns_on_device);
 /* Fill column `col` of an existing int32 object on the device with the seeded
  * counter-based generator: value(i) = lo + ((mix(seed, stream, row0 + i) >> 32)
  * * (hi - lo + 1)) >> 32 (splitmix64 output function), i.e. rows row0.. of an
@@ -118,7 +135,10 @@ svm_status svm_object_view(svm_ctx* ctx, const char* id, const char* base,
                            unsigned long long row0, unsigned long long nrows);
 svm_status svm_object_info(svm_ctx* ctx, const char* id, int* ncols, unsigned long long* nrows);
 svm_status svm_object_types(svm_ctx* ctx, const char* id, int* types, int max_cols);
-/* Copy rows [row0, row0 + n) of column `col` to host memory (4 or 8 bytes per value). */
+/* Type and width (val_size: 4 / 8, or a String column's bytes per value) of each column. */
+svm_status svm_object_columns(svm_ctx* ctx, const char* id, svm_column_desc* cols, int max_cols);
+/* Copy rows [row0, row0 + n) of column `col` to host memory (4 or 8 bytes per
+ * value; val_size bytes per value for a String column, NUL-padded). */
 svm_status svm_object_read(svm_ctx* ctx, const char* id, int col, unsigned long long row0,
                            unsigned long long n, void* host_out);
 /* Device address of column `col` (valid until the object is dropped/replaced). */
@@ -155,11 +175,6 @@ typedef struct svm_arg {
   const char* key;   /* OperatorInfo.args key: predication, select, lkey, rkey, dim, metric ... */
   const char* value;
 } svm_arg;
-
-typedef struct svm_column_desc { /* ColumnInfo (svm.proto:73-79) */
-  int type;                      /* SVM_INT32, SVM_INT64, SVM_STRING ... */
-  long long val_size;
-} svm_column_desc;
 
 typedef struct svm_operator {    /* OperatorInfo (svm.proto:101-123) */
   int type;                      /* SVM_OP_* */

@@ -135,6 +135,13 @@ def _driver(mode: str) -> ctypes.CDLL:
 _NP = {ValType.Int32: np.int32, ValType.Int64: np.int64, ValType.Int16: np.int16}
 
 
+def _dtype(col) -> np.dtype:
+    """NumPy type of a column: its int type, or val_size raw bytes for a String."""
+    if col.type == ValType.String:
+        return np.dtype(f"S{int(col.val_size)}")
+    return np.dtype(_NP[col.type])
+
+
 def _view(addr: int, dtype, n: int) -> np.ndarray:
     if n == 0:
         return np.zeros(0, dtype)
@@ -174,7 +181,7 @@ class Obj:
             if b < 0:
                 raise MemoryError("oracle bulk allocation failed")
             for c, arr in enumerate(cols):
-                t = _NP[schema.column_list[c].type]
+                t = _dtype(schema.column_list[c])
                 dst = _view(o.lib.svmo_bulk_column(o.h, b, c), t, cnt)
                 dst[:] = np.asarray(arr[b0:b0 + cnt], dtype=t)
         return o
@@ -183,13 +190,13 @@ class Obj:
         return self.lib.svmo_object_nbulks(self.h)
 
     def column(self, bulk: int, col: int) -> np.ndarray:
-        t = _NP[self.schema.column_list[col].type]
+        t = _dtype(self.schema.column_list[col])
         n = self.lib.svmo_bulk_tuple_count(self.h, bulk)
         return _view(self.lib.svmo_bulk_column(self.h, bulk, col), t, n).copy()
 
     def concat(self, col: int) -> np.ndarray:
         return np.concatenate([self.column(b, col) for b in range(self.nbulks())]) if self.nbulks() else \
-            np.zeros(0, _NP[self.schema.column_list[col].type])
+            np.zeros(0, _dtype(self.schema.column_list[col]))
 
 
 # ------------------------------------------------------------------ codegen
@@ -226,7 +233,11 @@ def compile_query(code: str, mode: str) -> str:
     """Compile generated host code with the reference's flags; cached by hash."""
     d = os.path.join(BUILD if mode == "port" else REF, "q")
     os.makedirs(d, exist_ok=True)
-    h = hashlib.sha1(code.encode()).hexdigest()[:20]
+    key = code
+    if mode == "port":  # a changed runtime header recompiles
+        with open(os.path.join(HERE, "svm_port_runtime.h")) as f:
+            key += f.read()
+    h = hashlib.sha1(key.encode()).hexdigest()[:20]
     so = os.path.join(d, f"q{h}.so")
     if not os.path.exists(so):
         src = os.path.join(d, f"q{h}.cpp")
@@ -319,9 +330,9 @@ def run_workload(w, mode: str = "port", threads: int = 1, fact: list | None = No
     path: the dimension pipelines, then the fact pipeline, as the reference's
     drivers run them (example/run_SSB_Q31.cu:77-107).  Returns
     ((keys, sums), RunStats of the fact pipeline)."""
-    from shadowvm_gb300.workloads import int_schema
+    from shadowvm_gb300.workloads import schema_of
     tpb = w.tuple_per_bulk
-    objs = {name: Obj.from_columns(cols, int_schema(len(cols)), tpb, mode) for name, cols in w.dims.items()}
+    objs = {name: Obj.from_columns(cols, schema_of(cols), tpb, mode) for name, cols in w.dims.items()}
     fact = w.fact_host(0, w.fact_rows) if fact is None else fact
     objs["lineorder"] = Obj.from_columns(fact, w.fact_schema(), tpb, mode)
     for p in w.dim_pipelines:

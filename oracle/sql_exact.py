@@ -8,6 +8,13 @@ comparisons and && || giving 0/1), the semantics the reference's generated C
 code has (codegen/codegen.cpp:240-277).  A join matches a key's FIRST row in
 the joined object, as the reference's Probe returns the first inserted match
 (com/cpp/cpu-runtime.hpp:125-138).
+
+String columns are NumPy fixed-width byte arrays ('S<w>', w = the column's
+val_size).  StrCmp(col, "lit", n) follows cpu-runtime.hpp:37-45 (compare at
+most n bytes, stop at a NUL on either side, signed chars); a String ReduceBy
+key is Hash(value, w) (cpu-runtime.hpp:68-74, signed chars); Map copies a
+String into its output width, cut or NUL-padded (the reference's StrCopy
+reads the following rows' bytes when the output is wider).
 """
 from __future__ import annotations
 
@@ -22,10 +29,48 @@ _TOK = re.compile(r"\s*(\$\(\s*\d+\s*\.\s*\d+\s*\)|0[xX][0-9a-fA-F]+|\d+|<<|>>|<
 _LEVELS = [["|"], ["^"], ["&"], ["==", "!="], ["<", "<=", ">", ">="], ["<<", ">>"], ["+", "-"], ["*", "/", "%"]]
 
 
+class Lit(str):
+    """A string literal token."""
+
+
 def tokenize(s: str) -> list[str]:
     out, i = [], 0
     s = s.rstrip()
     while i < len(s):
+        while i < len(s) and s[i].isspace():
+            i += 1
+        if i >= len(s):
+            break
+        if s[i] == '"' or s.startswith('\\"', i):  # "lit" or \"lit\" (the Java DSL's form)
+            esc = s[i] == "\\"
+            j = i + (2 if esc else 1)
+            v = []
+            while True:
+                if j >= len(s):
+                    raise ValueError("unterminated string literal")
+                if esc and s.startswith('\\"', j):
+                    j += 2
+                    break
+                if not esc and s[j] == '"':
+                    j += 1
+                    break
+                if s[j] == "\\" and j + 1 < len(s):
+                    v.append({"0": "\0", "n": "\n", "t": "\t"}.get(s[j + 1], s[j + 1]))
+                    j += 2
+                    continue
+                v.append(s[j])
+                j += 1
+            out.append(Lit("".join(v)))
+            i = j
+            continue
+        if s.startswith("StrCmp", i):
+            out.append("StrCmp")
+            i += 6
+            continue
+        if s[i] == ",":
+            out.append(",")
+            i += 1
+            continue
         m = _TOK.match(s, i)
         if not m:
             raise ValueError(f"cannot tokenize {s[i:]!r}")
@@ -88,6 +133,16 @@ def parse(s: str):
 
     def primary():
         t = take()
+        if t == "StrCmp" and not isinstance(t, Lit):
+            assert take() == "("
+            col = cond()
+            assert take() == ","
+            lit = take()
+            assert isinstance(lit, Lit), "StrCmp's second argument must be a string literal"
+            assert take() == ","
+            n = cond()
+            assert take() == ")"
+            return ("strcmp", col, str(lit), n)
         if t == "(":
             a = cond()
             assert take() == ")"
@@ -111,13 +166,59 @@ def _i32(x):
     return np.asarray(x, dtype=np.int64).astype(np.int32)
 
 
+def _sbytes(v: bytes, i: int) -> int:
+    return (v[i] ^ 0x80) - 0x80 if i < len(v) else 0  # signed char, NUL past the value
+
+
+def strcmp_value(v: bytes, width: int, lit: str, n: int) -> int:
+    """StrCmp(value, lit, n) of a value of `width` bytes (cpu-runtime.hpp:37-45)."""
+    lb = lit.encode("utf-8")  # the bytes the pipeline's text carries
+    for i in range(n):
+        if i >= width:
+            raise ValueError("unsupported: StrCmp reads past the column's width (the next row's bytes)")
+        a, b = _sbytes(v, i), _sbytes(lb, i)
+        if a == 0 or b == 0:
+            return 0
+        if a != b:
+            return a - b
+    return 0
+
+
+def hash_value(v: bytes, width: int) -> int:
+    """Hash(value, width) (cpu-runtime.hpp:68-74), signed chars."""
+    h = 0
+    for i in range(width):
+        h = (h * 31 + _sbytes(v, i)) & 0xFFFFFFFF
+    return h & 0x7FFFFFFF
+
+
+def _per_value(arr: np.ndarray, fn) -> np.ndarray:
+    """fn over the distinct values of a String array, mapped back to rows."""
+    uniq, inv = np.unique(arr, return_inverse=True)
+    vals = np.array([fn(bytes(u)) for u in uniq], np.int64)
+    return vals[inv.reshape(-1)] if len(arr) else np.zeros(0, np.int64)
+
+
+def _num(a: np.ndarray) -> np.ndarray:
+    if a.dtype.kind == "S":
+        raise ValueError("unsupported: a String column used as a number")
+    return a
+
+
 def evaluate(tree, env, n: int) -> np.ndarray:
-    """env[(obj, col)] -> int32 array of length n."""
+    """env[(obj, col)] -> int32 array (or 'S<w>' bytes for a String column) of length n."""
     op = tree[0]
     if op == "const":
         return np.full(n, tree[1], np.int64).astype(np.int32)
     if op == "col":
-        return env[(tree[1], tree[2])]
+        return _num(env[(tree[1], tree[2])])
+    if op == "strcmp":
+        col = env[(tree[1][1], tree[1][2])]
+        if tree[1][0] != "col" or col.dtype.kind != "S":
+            raise ValueError("unsupported: StrCmp of a column that is not a String")
+        nn = int(evaluate(tree[3], env, 1)[0])
+        w = col.dtype.itemsize
+        return _per_value(col, lambda v: strcmp_value(v, w, tree[2], nn)).astype(np.int32)
     if op == "?":
         c = evaluate(tree[1], env, n)
         return np.where(c != 0, evaluate(tree[2], env, n), evaluate(tree[3], env, n)).astype(np.int32)
@@ -174,14 +275,27 @@ def _keyref(s: str) -> tuple[int, int]:
     return int(m.group(1)), int(m.group(2))
 
 
+def _col(v) -> np.ndarray:
+    a = np.asarray(v)
+    return a if a.dtype.kind == "S" else a.astype(np.int32)
+
+
 def run_select(p: PipelineInfo, cols: list[np.ndarray]) -> list[np.ndarray]:
     filt, sel, *_ = _bind(p)
     n = len(cols[0]) if cols else 0
-    env = {(0, c): np.asarray(v, np.int32) for c, v in enumerate(cols)}
+    env = {(0, c): _col(v) for c, v in enumerate(cols)}
     mask = np.ones(n, bool)
     if filt:
         mask = evaluate(parse("&&".join(filt)), env, n) != 0
-    return [evaluate(parse(e), env, n)[mask] for e in sel]
+    out_schema = [op.output for op in p.workflow if op.type == OpType.Map][0].column_list
+    res = []
+    for i, e in enumerate(sel):
+        t = parse(e)
+        if t[0] == "col" and env[(t[1], t[2])].dtype.kind == "S":  # a String copy into its output width
+            res.append(env[(t[1], t[2])][mask].astype(f"S{int(out_schema[i].val_size)}"))
+        else:
+            res.append(evaluate(t, env, n)[mask])
+    return res
 
 
 def first_match(dim_keys: np.ndarray, probe: np.ndarray) -> np.ndarray:
@@ -204,19 +318,19 @@ def run_reduce(p: PipelineInfo, fact: list[np.ndarray], dims: list[list[np.ndarr
     nk = len(keyexp)
     if n == 0:
         return np.zeros((0, nk), np.int32), np.zeros((0, len(met)), np.int64)
-    env = {(0, c): np.asarray(v, np.int32) for c, v in enumerate(fact)}
+    env = {(0, c): _col(v) for c, v in enumerate(fact)}
     mask = np.ones(n, bool)
     if filt:
         mask = evaluate(parse("&&".join(filt)), env, n) != 0
     for lk, rk in joins:
         lo, lc = _keyref(lk)
         ro, rc = _keyref(rk)
-        idx = first_match(np.asarray(dims[ro - 1][rc], np.int32), env[(lo, lc)])
+        idx = first_match(np.asarray(dims[ro - 1][rc], np.int32), _num(env[(lo, lc)]))
         mask &= idx >= 0
         safe = np.where(idx >= 0, idx, 0)
         for c, col in enumerate(dims[ro - 1]):
-            col = np.asarray(col, np.int32)
-            env[(ro, c)] = col[safe] if len(col) else np.zeros(n, np.int32)
+            col = _col(col)
+            env[(ro, c)] = col[safe] if len(col) else np.zeros(n, col.dtype)
     sub = {k: v[mask] for k, v in env.items()}
     m = int(mask.sum())
     vals = [evaluate(parse(e), sub, m).astype(np.int64) for e in met]
@@ -226,7 +340,13 @@ def run_reduce(p: PipelineInfo, fact: list[np.ndarray], dims: list[list[np.ndarr
         sums = [int(v.sum(dtype=np.int64)) for v in vals]
         sums = [s if w else int(np.int64(s).astype(np.int32)) for s, w in zip(sums, metric_wide)]
         return np.zeros((1, 0), np.int32), np.array([sums], np.int64)
-    keys = np.stack([sub[_keyref(e)] for e in keyexp], axis=1) if m else np.zeros((0, nk), np.int32)
+    def key(e):  # a String key is its Hash over the column's width
+        a = sub[_keyref(e)]
+        if a.dtype.kind == "S":
+            w = a.dtype.itemsize
+            return _per_value(a, lambda v: hash_value(v, w)).astype(np.int32)
+        return a
+    keys = np.stack([key(e) for e in keyexp], axis=1) if m else np.zeros((0, nk), np.int32)
     if m == 0:
         return np.zeros((0, nk), np.int32), np.zeros((0, len(met)), np.int64)
     uniq, inv = np.unique(keys, axis=0, return_inverse=True)

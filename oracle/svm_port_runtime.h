@@ -9,9 +9,10 @@
  * header or against the reference's own headers (oracle/_ref); the two builds
  * are compared by the oracle tests.
  *
- * Signedness: the reference hashes key bytes through plain `char`, which is
- * signed on x86 and unsigned on aarch64.  This header fixes the x86 behaviour
- * (signed) on every host; define SVM_PORT_UNSIGNED_CHAR to get the aarch64 one.
+ * Signedness: the reference hashes and compares key bytes through plain
+ * `char`, which is signed on x86 and unsigned on aarch64.  This header fixes
+ * the x86 behaviour (signed) on every host, for Hash and StrCmp alike; define
+ * SVM_PORT_UNSIGNED_CHAR to get the aarch64 one.
  */
 #ifndef SVM_PORT_RUNTIME_H_
 #define SVM_PORT_RUNTIME_H_
@@ -99,11 +100,15 @@ inline unsigned Hash(const char* p, int n) {
   return h & 0x7FFFFFFFu;
 }
 
-/* cpu-runtime.hpp:37-44: compare at most n bytes, stopping at either NUL. */
+/* cpu-runtime.hpp:37-44: compare at most n bytes, stopping at either NUL;
+ * the difference of the first unequal bytes, as chars of the same
+ * signedness as Hash's. */
 inline int StrCmp(const char* a, const char* b, int n) {
+  const svm_hash_byte* x = (const svm_hash_byte*)a;
+  const svm_hash_byte* y = (const svm_hash_byte*)b;
   for (int k = 0; k < n; k++) {
-    if (a[k] == '\0' || b[k] == '\0') return 0;
-    if (a[k] != b[k]) return a[k] - b[k];
+    if (x[k] == 0 || y[k] == 0) return 0;
+    if (x[k] != y[k]) return (int)x[k] - (int)y[k];
   }
   return 0;
 }

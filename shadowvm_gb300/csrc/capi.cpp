@@ -5,6 +5,7 @@
 
 #include "ctx.h"
 #include "kernels.h"
+#include "strdict.h"
 
 namespace svm {
 
@@ -159,9 +160,10 @@ svm_status Ctx::scratch_take(size_t bytes, void** out) {
 }
 
 svm_status Ctx::column_stats(const ObjectPtr& o, int c, ColStats* out) {
-  if ((int)o->stats.size() < o->ncols) o->stats.resize(o->ncols);
+  if (o->stats.size() < o->types.size()) o->stats.resize(o->types.size());
   if (!o->stats[c].valid) {
-    if (o->types[c] != SVM_INT32) return fail(SVM_E_UNSUPPORTED, "column statistics need an int32 column");
+    if (o->types[c] != SVM_INT32 && o->types[c] != SVM_STRING)
+      return fail(SVM_E_UNSUPPORTED, "column statistics need an int32 column");
     int32_t h[2] = {INT_MAX, INT_MIN};
     DevBufPtr d;
     svm_status st = alloc(8, &d);
@@ -299,9 +301,9 @@ void* svm_stream(svm_ctx* c) { return c ? (void*)c->impl.stream : nullptr; }
 
 unsigned long long svm_bytes_in_use(const svm_ctx* c) { return c ? c->impl.in_use : 0; }
 
-svm_status svm_object_put(svm_ctx* c, const char* id, int ncols, const int* types,
-                          unsigned long long nrows, const void* const* columns, int on_device) {
-  if (!c || !id || ncols <= 0 || ncols > 64 || !types) return SVM_E_INVALID_ARG;
+svm_status svm_object_put_columns(svm_ctx* c, const char* id, int ncols, const svm_column_desc* cols,
+                                  unsigned long long nrows, const void* const* columns, int on_device) {
+  if (!c || !id || ncols <= 0 || ncols > 64 || !cols) return SVM_E_INVALID_ARG;
   Ctx* x = C(c);
   std::lock_guard<std::recursive_mutex> g(x->mu);
   cudaSetDevice(x->device);
@@ -314,17 +316,24 @@ svm_status svm_object_put(svm_ctx* c, const char* id, int ncols, const int* type
   o->bulk0_rows = nrows < x->cfg.tuple_per_bulk ? nrows : x->cfg.tuple_per_bulk;
   o->source_rows = nrows;
   unsigned long long padded = (nrows + 63) / 64 * 64 + 64;
+  for (int k = 0; k < ncols; k++) {
+    const int t = cols[k].type;
+    if (t != SVM_INT32 && t != SVM_INT64 && t != SVM_STRING)
+      return x->fail(SVM_E_UNSUPPORTED, "object columns must be Int32, Int64 or String");
+    if (t == SVM_STRING && (cols[k].val_size <= 0 || cols[k].val_size > 4096))
+      return x->fail(SVM_E_INVALID_ARG, "a String column needs a width (val_size) of 1..4096 bytes");
+  }
   // Replacing an object of the same shape that no view shares: reuse its storage.
   ObjectPtr old = x->find(id);
-  bool reuse = old && old->ncols == ncols && old->nrows == nrows && old->row0 == 0;
+  bool reuse = old && old->ncols == ncols && old->nrows == nrows && old->row0 == 0 &&
+               (int)old->storage.size() == ncols;
   for (int k = 0; reuse && k < ncols; k++)
-    reuse = old->types[k] == types[k] && old->storage[k].use_count() == 1;
+    reuse = old->types[k] == cols[k].type && old->storage[k].use_count() == 1;
   for (int k = 0; k < ncols; k++) {
-    if (types[k] != SVM_INT32 && types[k] != SVM_INT64)
-      return x->fail(SVM_E_UNSUPPORTED, "object columns must be Int32 or Int64");
-    o->types.push_back(types[k]);
+    const int t = cols[k].type;
+    o->types.push_back(t);
     svm::DevBufPtr b;
-    size_t el = types[k] == SVM_INT64 ? 8 : 4;
+    size_t el = t == SVM_INT64 ? 8 : 4;  // String columns hold int32 dictionary codes
     if (reuse) {
       b = old->storage[k];
       if (!(columns && columns[k] && nrows)) {
@@ -335,7 +344,31 @@ svm_status svm_object_put(svm_ctx* c, const char* id, int ncols, const int* type
       svm_status st = x->alloc(padded * el, &b, true);
       if (st) return st;
     }
-    if (columns && columns[k] && nrows) {
+    if (t == SVM_STRING) {
+      // Dictionary-encode the fixed-width values (a device column arrives
+      // on the host first); a column left unset holds the all-NUL value.
+      const int w = (int)cols[k].val_size;
+      svm::StrCol sc;
+      sc.width = w;
+      std::vector<int32_t> codes;
+      if (columns && columns[k] && nrows) {
+        std::vector<char> hostv;
+        const char* vals = (const char*)columns[k];
+        if (on_device) {
+          hostv.resize(nrows * (size_t)w);
+          cudaError_t e = cudaMemcpy(hostv.data(), vals, hostv.size(), cudaMemcpyDeviceToHost);
+          if (e) return x->cuda_fail(e, "string column read");
+          vals = hostv.data();
+        }
+        sc.dict = svm::build_dict(vals, nrows, w, &codes);
+        svm_status st = x->upload(b->p, codes.data(), nrows * 4);
+        if (st) return st;
+      } else {  // every row the all-NUL value, code 0 (the storage is zeroed)
+        std::vector<char> zero((size_t)w, 0);
+        sc.dict = svm::build_dict(zero.data(), 1, w, &codes);
+      }
+      o->strs[k] = sc;
+    } else if (columns && columns[k] && nrows) {
       if (on_device) {
         cudaError_t e = cudaMemcpyAsync(b->p, columns[k], nrows * el, cudaMemcpyDeviceToDevice, x->stream);
         if (e) return x->cuda_fail(e, "cudaMemcpyAsync");
@@ -350,6 +383,18 @@ svm_status svm_object_put(svm_ctx* c, const char* id, int ncols, const int* type
   if (e) return x->cuda_fail(e, "object upload");
   x->objects[id] = o;
   return SVM_OK;
+}
+
+svm_status svm_object_put(svm_ctx* c, const char* id, int ncols, const int* types,
+                          unsigned long long nrows, const void* const* columns, int on_device) {
+  if (!c || !id || ncols <= 0 || ncols > 64 || !types) return SVM_E_INVALID_ARG;
+  std::vector<svm_column_desc> cols(ncols);
+  for (int k = 0; k < ncols; k++) {
+    if (types[k] != SVM_INT32 && types[k] != SVM_INT64)
+      return C(c)->fail(SVM_E_UNSUPPORTED, "object columns must be Int32 or Int64 (String columns: svm_object_put_columns)");
+    cols[k] = svm_column_desc{types[k], types[k] == SVM_INT64 ? 8 : 4};
+  }
+  return svm_object_put_columns(c, id, ncols, cols.data(), nrows, columns, on_device);
 }
 
 svm_status svm_object_load_text(svm_ctx* c, const char* id, int ncols, const int* types, const char* text,
@@ -513,9 +558,39 @@ svm_status svm_object_read(svm_ctx* c, const char* id, int col, unsigned long lo
     return x->fail(SVM_E_INVALID_ARG, "read out of range");
   if (!n) return SVM_OK;
   size_t el = o->elem(col);
+  if (o->is_string(col)) {  // codes back to fixed-width values (NUL-padded to the column's width)
+    std::vector<int32_t> codes(n);
+    cudaError_t e = cudaMemcpyAsync(codes.data(), o->col(col) + row0 * el, n * el, cudaMemcpyDeviceToHost, x->stream);
+    if (!e) e = cudaStreamSynchronize(x->stream);
+    if (e) return x->cuda_fail(e, "object read");
+    const svm::StrCol& sc = o->strs.at(col);
+    const int w = sc.width, dw = sc.dict->width < w ? sc.dict->width : w;
+    char* out = (char*)host_out;
+    for (unsigned long long i = 0; i < n; i++) {
+      char* dst = out + i * (unsigned long long)w;
+      const uint32_t k = (uint32_t)codes[i];
+      if (k >= sc.dict->count) return x->fail(SVM_E_DEVICE, "string code out of its dictionary");
+      std::memcpy(dst, sc.dict->value(k), (size_t)dw);
+      std::memset(dst + dw, 0, (size_t)(w - dw));
+    }
+    return SVM_OK;
+  }
   cudaError_t e = cudaMemcpyAsync(host_out, o->col(col) + row0 * el, n * el, cudaMemcpyDeviceToHost, x->stream);
   if (!e) e = cudaStreamSynchronize(x->stream);
   if (e) return x->cuda_fail(e, "object read");
+  return SVM_OK;
+}
+
+svm_status svm_object_columns(svm_ctx* c, const char* id, svm_column_desc* cols, int max_cols) {
+  if (!c || !id || !cols) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  ObjectPtr o = x->find(id);
+  if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
+  for (int k = 0; k < o->ncols && k < max_cols; k++) {
+    cols[k].type = o->types[k];
+    cols[k].val_size = o->is_string(k) ? o->strs.at(k).width : (long long)o->elem(k);
+  }
   return SVM_OK;
 }
 
@@ -573,6 +648,9 @@ svm_status svm_objects_read(svm_ctx* c, int n, const char* const* ids, void* hos
     if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + (ids[k] ? ids[k] : "(null)"));
     nrows_out[k] = o->nrows;
     for (int col = 0; col < o->ncols; col++) {
+      if (o->is_string(col))
+        return x->fail(SVM_E_UNSUPPORTED, std::string("objects read: ") + ids[k] +
+                                              " has a String column (read it with svm_object_read)");
       const unsigned long long bytes = o->nrows * o->elem(col);
       if (bytes) segs.push_back(svm::Segment{(const uint32_t*)o->col(col), total / 4, bytes / 4});
       total += (bytes + 7) & ~7ull;

@@ -32,6 +32,30 @@ struct ColStats {
   int32_t min = 0, max = 0;
 };
 
+// The distinct values of a String column (fixed width, as the reference's
+// ValType String, com/svm.proto:62-72), sorted by memcmp: the column stores
+// each row's int32 code, the value's position here.  Sorted codes keep the
+// values a StrCmp prefix comparison accepts contiguous.
+struct StrDict {
+  int width = 0;              // bytes per stored value
+  uint32_t count = 0;
+  std::vector<char> bytes;    // count x width
+  const char* value(uint32_t k) const { return bytes.data() + (size_t)k * width; }
+};
+using StrDictPtr = std::shared_ptr<const StrDict>;
+
+// A String column of an object: its declared width (the reference's
+// val_size: a value is its dictionary bytes followed by NULs up to it), its
+// dictionary, and -- once a ReduceBy has used it as a key -- the derived
+// int32 column holding each row's rank among the distinct Hash values
+// (cpu-runtime.hpp:68-74) and the Hash value of each rank.
+struct StrCol {
+  int width = 0;
+  StrDictPtr dict;
+  int rank_col = -1;
+  std::vector<int32_t> rank_hash;
+};
+
 // A columnar object.  Columns are int32 or int64; each column's storage is
 // padded to a multiple of 64 rows (+64 rows) so the scan's 16-byte group loads
 // never leave the allocation.  A view shares its base object's storage.
@@ -51,7 +75,12 @@ struct Object {
   // source); estimates how selective a join against it is.
   unsigned long long source_rows = 0;
   std::vector<ColStats> stats;
+  // String columns (types[c] == SVM_STRING: storage holds int32 codes).
+  // Derived columns (hash ranks) follow the ncols visible ones in types and
+  // storage.
+  std::map<int, StrCol> strs;
 
+  bool is_string(int c) const { return c >= 0 && c < (int)types.size() && types[c] == SVM_STRING; }
   char* base(int c) const { return (char*)storage[c]->p; }
   size_t elem(int c) const { return types[c] == SVM_INT64 ? 8 : 4; }
   char* col(int c) const { return base(c) + row0 * elem(c); }

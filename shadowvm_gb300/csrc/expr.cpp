@@ -8,7 +8,7 @@ namespace svm {
 
 namespace {
 
-enum TokKind { T_END, T_NUM, T_COL, T_OP, T_LP, T_RP };
+enum TokKind { T_END, T_NUM, T_COL, T_OP, T_LP, T_RP, T_COMMA, T_STR, T_CALL };
 
 struct Tok {
   TokKind kind;
@@ -96,11 +96,55 @@ class Lexer {
       }
       size_t k = j;
       while (k < s_.size() && isspace((unsigned char)s_[k])) k++;
-      if (k < s_.size() && s_[k] == '(')
-        return fail(err, "unsupported: function call " + id + "(...) (string/UDF expressions)");
+      if (k < s_.size() && s_[k] == '(') {
+        // StrCmp (com/cpp/cpu-runtime.hpp:37-45) is resolved against the
+        // column's dictionary by the planner; other calls (UDFs) are not.
+        if (id != "StrCmp") return fail(err, "unsupported: function call " + id + "(...) (UDF expressions)");
+        t->kind = T_CALL;
+        t->op = id;
+        i_ = j;
+        return true;
+      }
       return fail(err, "unsupported: identifier '" + id + "'");
     }
-    if (c == '"' || c == '\'') return fail(err, "unsupported: string/char literal");
+    if (c == ',') {
+      t->kind = T_COMMA;
+      i_++;
+      return true;
+    }
+    // A string literal, its quotes optionally backslash-escaped as the Java
+    // DSL writes them (StrCmp($p_category,\"MFGR#12\",8)); C escapes \\ \" \0.
+    if (c == '"' || (c == '\\' && i_ + 1 < s_.size() && s_[i_ + 1] == '"')) {
+      const bool escaped = c == '\\';
+      size_t j = i_ + (escaped ? 2 : 1);
+      std::string v;
+      for (;;) {
+        if (j >= s_.size()) return fail(err, "syntax: unterminated string literal");
+        if (escaped && s_[j] == '\\' && j + 1 < s_.size() && s_[j + 1] == '"') {
+          j += 2;
+          break;
+        }
+        if (!escaped && s_[j] == '"') {
+          j++;
+          break;
+        }
+        if (s_[j] == '\\' && j + 1 < s_.size()) {
+          const char e = s_[j + 1];
+          if (e == '0') v.push_back('\0');
+          else if (e == 'n') v.push_back('\n');
+          else if (e == 't') v.push_back('\t');
+          else v.push_back(e);
+          j += 2;
+          continue;
+        }
+        v.push_back(s_[j++]);
+      }
+      t->kind = T_STR;
+      t->op = v;
+      i_ = j;
+      return true;
+    }
+    if (c == '\'') return fail(err, "unsupported: char literal");
     static const char* two[] = {"<<", ">>", "<=", ">=", "==", "!=", "&&", "||"};
     for (const char* op : two) {
       if (s_.compare(i_, 2, op) == 0) {
@@ -269,6 +313,26 @@ class Parser {
       if (tok_.kind != T_RP) return fail("syntax: expected ')'");
       return advance();
     }
+    if (tok_.kind == T_CALL) {  // StrCmp(column, "literal", n)
+      if (!advance() || tok_.kind != T_LP) return fail("syntax: expected '(' after StrCmp");
+      int col, n;
+      if (!advance() || !cond(&col)) return false;
+      if (tok_.kind != T_COMMA) return fail("syntax: expected ',' in StrCmp");
+      if (!advance() || tok_.kind != T_STR) return fail("unsupported: StrCmp's second argument must be a string literal");
+      std::string lit = tok_.op;
+      if (!advance() || tok_.kind != T_COMMA) return fail("syntax: expected ',' in StrCmp");
+      if (!advance() || !cond(&n)) return false;
+      if (tok_.kind != T_RP) return fail("syntax: expected ')' after StrCmp's arguments");
+      if (e_->nodes[col].kind != N_COL) return fail("unsupported: StrCmp's first argument must be a column");
+      Node nd{N_STRCMP};
+      nd.a = col;
+      nd.b = n;
+      nd.value = (int32_t)e_->strs.size();
+      e_->strs.push_back(lit);
+      *out = add(nd);
+      return advance();
+    }
+    if (tok_.kind == T_STR) return fail("unsupported: a string literal outside StrCmp");
     if (tok_.kind == T_END) return fail("syntax: unexpected end of expression");
     return fail("syntax: unexpected token '" + tok_.op + "'");
   }
@@ -362,6 +426,9 @@ struct Emitter {
         p->arg[jpos] = (uint8_t)p->n;
         return true;
       }
+      case N_STRCMP:
+        *err = "unsupported: StrCmp left after string resolution";
+        return false;
       case N_COND: {
         if (!node(e, n.a)) return false;
         int jz = p->n;

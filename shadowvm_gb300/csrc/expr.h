@@ -7,9 +7,11 @@
 // same strings as C integer expressions over int32 columns into a tree, and
 // the planner maps the tree onto the kernels' compile-time functors (range
 // conjuncts, operand/binary metrics) or, for anything else inside the
-// grammar, onto a short bytecode program the kernels interpret.  Calls
-// (StrCmp, UDFs), floating point and string literals are reported as
-// unsupported -- there is no fallback path.
+// grammar, onto a short bytecode program the kernels interpret.
+// StrCmp(column, "literal", n) parses into an N_STRCMP node that the planner
+// resolves against the column's dictionary (strdict.h) before planning;
+// other calls (UDFs), floating point and string literals elsewhere are
+// reported as unsupported -- there is no fallback path.
 #pragma once
 
 #include <string>
@@ -26,7 +28,8 @@ struct ColRef {
   bool operator<(const ColRef& o) const { return obj != o.obj ? obj < o.obj : col < o.col; }
 };
 
-enum NodeKind { N_COL, N_CONST, N_UNARY, N_BINARY, N_LAND, N_LOR, N_COND };
+enum NodeKind { N_COL, N_CONST, N_UNARY, N_BINARY, N_LAND, N_LOR, N_COND,
+                N_STRCMP };  // a = column node, b = length node, value = literal index
 
 struct Node {
   NodeKind kind;
@@ -38,6 +41,7 @@ struct Node {
 
 struct Expr {
   std::vector<Node> nodes;
+  std::vector<std::string> strs;  // StrCmp literals
   int root = -1;
 };
 

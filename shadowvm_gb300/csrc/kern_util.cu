@@ -220,4 +220,38 @@ cudaError_t launch_gather_segments(const Segment* segs, int nseg, uint32_t* dst,
   return cudaGetLastError();
 }
 
+// out[i] = lut[in[i]] (dictionary code -> hash rank, hash rank -> hash value;
+// in and out may be the same array).
+__global__ void lut_gather_kernel(const int32_t* in, unsigned long long n, const int32_t* lut, int32_t* out) {
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x)
+    out[i] = lut[in[i]];
+}
+
+cudaError_t launch_lut_gather(const int32_t* in, unsigned long long n, const int32_t* lut, int32_t* out,
+                              cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const unsigned long long want = (n + 255) / 256;
+  const unsigned long long cap = (unsigned long long)num_sms() * 8;
+  note_launch();
+  lut_gather_kernel<<<(unsigned)(want < cap ? want : cap), 256, 0, s>>>(in, n, lut, out);
+  return cudaGetLastError();
+}
+
+// flags[codes[i]] = 1: which dictionary codes a column holds.
+__global__ void mark_codes_kernel(const int32_t* codes, unsigned long long n, uint32_t* flags) {
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x)
+    flags[codes[i]] = 1u;
+}
+
+cudaError_t launch_mark_codes(const int32_t* codes, unsigned long long n, uint32_t* flags, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const unsigned long long want = (n + 255) / 256;
+  const unsigned long long cap = (unsigned long long)num_sms() * 8;
+  note_launch();
+  mark_codes_kernel<<<(unsigned)(want < cap ? want : cap), 256, 0, s>>>(codes, n, flags);
+  return cudaGetLastError();
+}
+
 }  // namespace svm

@@ -38,6 +38,11 @@ struct Segment {
   unsigned long long words;
 };
 cudaError_t launch_gather_segments(const Segment* segs, int nseg, uint32_t* dst, cudaStream_t s);
+// flags[codes[i]] = 1 for i < n (flags zeroed by the caller; every code indexes flags).
+cudaError_t launch_mark_codes(const int32_t* codes, unsigned long long n, uint32_t* flags, cudaStream_t s);
+// out[i] = lut[in[i]] for i < n (in == out allowed); every in[i] indexes lut.
+cudaError_t launch_lut_gather(const int32_t* in, unsigned long long n, const int32_t* lut, int32_t* out,
+                              cudaStream_t s);
 
 // ---- select pipelines (kern_dim.cu)
 // Pass 1: per-tile counts of rows passing the conjuncts; pass 2: order-preserving write.

@@ -19,6 +19,7 @@
 #include "ctx.h"
 #include "expr.h"
 #include "kernels.h"
+#include "strdict.h"
 
 namespace svm {
 
@@ -31,6 +32,9 @@ struct Bound {
   bool is_reduce = false;
   bool has_map = false;
   std::vector<svm_column_desc> sink;
+  // Per ReduceBy key: for a String key (grouped by hash rank), the Hash value
+  // of each rank, written in place of the rank; empty otherwise.
+  std::vector<std::vector<int32_t>> key_hash;
 };
 
 const char* arg_of(const svm_operator& op, const char* key) {
@@ -186,12 +190,25 @@ svm_status run_select(Ctx* x, const Bound& b, const ObjectPtr& src) {
     if (r.obj != 0) return x->fail(SVM_E_INVALID_ARG, "Map/Filter references object " + std::to_string(r.obj) +
                                                           " but the pipeline joins nothing");
     if (r.col < 0 || r.col >= src->ncols) return x->fail(SVM_E_INVALID_ARG, "column out of range");
-    if (src->types[r.col] != SVM_INT32) return x->fail(SVM_E_UNSUPPORTED, "only int32 input columns");
+    // String columns are their int32 codes here: StrCmp tests were rewritten
+    // onto them, and a bare projection copies them.
+    if (src->types[r.col] != SVM_INT32 && src->types[r.col] != SVM_STRING)
+      return x->fail(SVM_E_UNSUPPORTED, "only int32 and String input columns");
   }
+  // A String output column is a bare String column of the source (StrCopy,
+  // codegen/codegen.cpp:169-170).
+  std::vector<int> str_src(b.select_exp.size(), -1);
   for (size_t i = 0; i < b.select_exp.size(); i++) {
     if (i >= b.sink.size()) return x->fail(SVM_E_INVALID_ARG, "Sink schema has fewer columns than the Map");
-    if (b.sink[i].type != SVM_INT32)
-      return x->fail(SVM_E_UNSUPPORTED, "projected columns must be declared Int32");
+    const Node& root = proj[i].nodes[proj[i].root];
+    const bool bare_str = root.kind == N_COL && src->is_string(root.ref.col);
+    if (b.sink[i].type == SVM_STRING) {
+      if (!bare_str) return x->fail(SVM_E_UNSUPPORTED, "a String output column must be a String input column");
+      if (b.sink[i].val_size <= 0) return x->fail(SVM_E_INVALID_ARG, "a String output column needs a width");
+      str_src[i] = root.ref.col;
+    } else if (b.sink[i].type != SVM_INT32 || bare_str) {
+      return x->fail(SVM_E_UNSUPPORTED, "projected columns must be declared Int32 (String for a String column)");
+    }
   }
   SelectParams sp{};
   sp.ncols_in = (int)opnds.size();
@@ -244,6 +261,32 @@ svm_status run_select(Ctx* x, const Bound& b, const ObjectPtr& src) {
   e = launch_select_write(sp, x->stream);
   x->prof_end(SVM_K_SELECT, ev);
   if (e) return x->cuda_fail(e, "select write");
+  // String outputs: the source's codes with its dictionary, or -- for a
+  // narrower output column -- recoded into the dictionary of the cut values.
+  // (A wider one is NUL-padded; the reference's StrCopy reads the next rows'
+  // bytes there.)
+  std::vector<DevBufPtr> luts;
+  for (size_t i = 0; i < str_src.size(); i++) {
+    if (str_src[i] < 0) continue;
+    const StrCol& in = src->strs.at(str_src[i]);
+    StrCol oc;
+    oc.width = (int)b.sink[i].val_size;
+    if (oc.width >= in.dict->width) {
+      oc.dict = in.dict;
+    } else {
+      std::vector<int32_t> remap;
+      oc.dict = truncate_dict(*in.dict, oc.width, &remap);
+      DevBufPtr lut;
+      if ((st = x->alloc(4 * remap.size() + 4, &lut))) return st;
+      if (!e) e = cudaMemcpy(lut->p, remap.data(), 4 * remap.size(), cudaMemcpyHostToDevice);
+      if (!e) e = launch_lut_gather((const int32_t*)out->col((int)i), out->nrows, (const int32_t*)lut->p,
+                                    (int32_t*)out->col((int)i), x->stream);
+      luts.push_back(lut);
+    }
+    out->types[i] = SVM_STRING;
+    out->strs[(int)i] = oc;
+  }
+  if (e) return x->cuda_fail(e, "string recode");
   if ((st = sync_and_check(x, "select write"))) return st;
   // Output bulk i holds the rows of source bulk i (core/pipeline.cu:161-162, 289-332).
   out->has_bulks = src->has_bulks;
@@ -470,17 +513,21 @@ svm_status plan_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::ve
     if (!parse_expr(b.metric_exp[m], &mexp[m], &err))
       return x->fail(err.rfind("unsupported", 0) == 0 ? SVM_E_UNSUPPORTED : SVM_E_INVALID_ARG,
                      "metric '" + b.metric_exp[m] + "': " + err);
+  // Column indices past ncols are derived columns (String keys' hash ranks);
+  // String columns themselves appear only as the codes StrCmp tests read.
   auto check_ref = [&](const ColRef& r, bool allow_dims) -> svm_status {
     if (r.obj == 0) {
-      if (r.col < 0 || r.col >= src->ncols) return x->fail(SVM_E_INVALID_ARG, "column out of range");
-      if (src->types[r.col] != SVM_INT32) return x->fail(SVM_E_UNSUPPORTED, "only int32 fact columns");
+      if (r.col < 0 || r.col >= (int)src->types.size()) return x->fail(SVM_E_INVALID_ARG, "column out of range");
+      if (src->types[r.col] != SVM_INT32 && src->types[r.col] != SVM_STRING)
+        return x->fail(SVM_E_UNSUPPORTED, "only int32 fact columns");
       return SVM_OK;
     }
     if (!allow_dims)
       return x->fail(SVM_E_UNSUPPORTED, "a Filter on a joined object (the reference evaluates filters before joins)");
     if (r.obj > nref || join_of_obj[r.obj] < 0)
       return x->fail(SVM_E_INVALID_ARG, "reference to object " + std::to_string(r.obj) + " that is not joined");
-    if (r.col < 0 || r.col >= refs[r.obj - 1]->ncols) return x->fail(SVM_E_INVALID_ARG, "column out of range");
+    if (r.col < 0 || r.col >= (int)refs[r.obj - 1]->types.size())
+      return x->fail(SVM_E_INVALID_ARG, "column out of range");
     return SVM_OK;
   };
   std::vector<ColRef> pred_refs, met_refs;
@@ -740,6 +787,26 @@ svm_status plan_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::ve
   return SVM_OK;
 }
 
+// Hash-rank keys back to the reference's Hash values (ranks order like the
+// hashes, so the rows stay sorted by key).
+svm_status translate_keys(Ctx* x, const Bound& b, const ObjectPtr& out) {
+  cudaError_t e = cudaSuccess;
+  std::vector<DevBufPtr> luts;
+  for (size_t q = 0; q < b.key_hash.size(); q++) {
+    if (b.key_hash[q].empty() || out->nrows == 0) continue;
+    DevBufPtr lut;
+    svm_status st = x->alloc(4 * b.key_hash[q].size(), &lut);
+    if (st) return st;
+    if (!e) e = cudaMemcpyAsync(lut->p, b.key_hash[q].data(), 4 * b.key_hash[q].size(), cudaMemcpyHostToDevice,
+                                x->stream);
+    if (!e) e = launch_lut_gather((const int32_t*)out->col((int)q), out->nrows, (const int32_t*)lut->p,
+                                  (int32_t*)out->col((int)q), x->stream);
+    luts.push_back(lut);
+  }
+  if (e) return x->cuda_fail(e, "string key translation");
+  return luts.empty() ? SVM_OK : sync_and_check(x, "string key translation");
+}
+
 svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs) {
   StarPlan plan;
   svm_status st = plan_star(x, b, src, refs, &plan);
@@ -835,6 +902,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
     x->prof_end(SVM_K_FINALIZE, ev);
     if (e) return x->cuda_fail(e, "finalize write");
     if ((st = sync_and_check(x, "finalize"))) return st;
+    if ((st = translate_keys(x, b, out))) return st;
   }
   out->has_bulks = true;
   out->bulk0_rows = out->nrows;
@@ -845,6 +913,93 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
 }  // namespace
 
 namespace {
+
+// The derived column of object o's String column c holding each row's rank
+// among the column's distinct Hash values (built once per object).
+svm_status ensure_rank_col(Ctx* x, const ObjectPtr& o, int c, int* idx) {
+  StrCol& sc = o->strs.at(c);
+  if (sc.rank_col >= 0) {
+    *idx = sc.rank_col;
+    return SVM_OK;
+  }
+  // The codes the column holds, then ranks over their hashes only.
+  const uint32_t D = sc.dict->count;
+  std::vector<uint32_t> present(D, 0);
+  DevBufPtr flags, lut, col;
+  svm_status st;
+  if ((st = x->alloc(4ull * D + 4, &flags, true))) return st;
+  cudaError_t e = launch_mark_codes((const int32_t*)o->col(c), o->nrows, (uint32_t*)flags->p, x->stream);
+  if (!e && D) e = cudaMemcpyAsync(present.data(), flags->p, 4ull * D, cudaMemcpyDeviceToHost, x->stream);
+  if (!e) e = cudaStreamSynchronize(x->stream);
+  if (e) return x->cuda_fail(e, "string key codes");
+  std::vector<int32_t> rank_of_code, hash_of_rank;
+  hash_ranks(*sc.dict, sc.width, present, &rank_of_code, &hash_of_rank);
+  const unsigned long long rows = o->row0 + o->nrows, padded = (rows + 63) / 64 * 64 + 64;
+  if ((st = x->alloc(4 * rank_of_code.size() + 4, &lut)) || (st = x->alloc(4 * padded, &col, true))) return st;
+  e = cudaMemcpyAsync(lut->p, rank_of_code.data(), 4 * rank_of_code.size(), cudaMemcpyHostToDevice, x->stream);
+  if (!e) e = launch_lut_gather((const int32_t*)o->col(c), o->nrows, (const int32_t*)lut->p,
+                                (int32_t*)col->p + o->row0, x->stream);
+  if (e) return x->cuda_fail(e, "string key ranks");
+  if ((st = sync_and_check(x, "string key ranks"))) return st;
+  o->types.push_back(SVM_INT32);
+  o->storage.push_back(col);
+  if (o->stats.size() < o->types.size()) o->stats.resize(o->types.size());
+  o->stats.back() = ColStats{true, 0, hash_of_rank.empty() ? 0 : (int32_t)hash_of_rank.size() - 1};
+  sc.rank_col = (int)o->types.size() - 1;
+  sc.rank_hash = std::move(hash_of_rank);
+  *idx = sc.rank_col;
+  return SVM_OK;
+}
+
+// String columns in a bound pipeline: StrCmp comparisons in Filter, Map and
+// metric expressions become tests of the codes; String ReduceBy keys become
+// their hash-rank columns (b->key_hash keeps the way back); String join keys
+// and any other use of a String column are unsupported.
+svm_status resolve_strings(Ctx* x, Bound* b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs) {
+  auto obj_of = [&](int k) -> ObjectPtr {
+    return k == 0 ? src : (k >= 1 && k <= (int)refs.size() ? refs[k - 1] : nullptr);
+  };
+  auto strcol = [&](const ColRef& r) -> const StrCol* {
+    ObjectPtr o = obj_of(r.obj);
+    if (!o || !o->is_string(r.col)) return nullptr;
+    auto it = o->strs.find(r.col);
+    return it == o->strs.end() ? nullptr : &it->second;
+  };
+  auto rewrite = [&](std::string* text, bool allow_bare, const char* what) -> svm_status {
+    Expr e;
+    std::string err;
+    if (!parse_expr(*text, &e, &err)) return SVM_OK;  // the planner reports it
+    if (allow_bare && e.nodes[e.root].kind == N_COL && strcol(e.nodes[e.root].ref)) return SVM_OK;
+    bool has = false;
+    for (const Node& n : e.nodes) has |= n.kind == N_STRCMP || (n.kind == N_COL && strcol(n.ref));
+    if (!has) return SVM_OK;
+    if (!rewrite_strings(&e, strcol, &err))
+      return x->fail(SVM_E_UNSUPPORTED, std::string(what) + " '" + *text + "': " + err);
+    *text = print_expr(e, e.root);
+    return SVM_OK;
+  };
+  svm_status st;
+  for (auto& f : b->filter_exp)
+    if ((st = rewrite(&f, false, "predication"))) return st;
+  for (auto& m : b->metric_exp)
+    if ((st = rewrite(&m, false, "metric"))) return st;
+  for (auto& sel : b->select_exp)
+    if ((st = rewrite(&sel, true, "select"))) return st;
+  for (size_t j = 0; j < b->join_lkey.size(); j++)
+    if (strcol(b->join_lkey[j]) || strcol(b->join_rkey[j]))
+      return x->fail(SVM_E_UNSUPPORTED, "String join keys are not supported (join on an int32 key)");
+  b->key_hash.assign(b->reduce_key.size(), {});
+  for (size_t q = 0; q < b->reduce_key.size(); q++) {
+    const ColRef r = b->reduce_key[q];
+    if (!strcol(r)) continue;
+    ObjectPtr o = obj_of(r.obj);
+    int idx;
+    if ((st = ensure_rank_col(x, o, r.col, &idx))) return st;
+    b->key_hash[q] = o->strs.at(r.col).rank_hash;
+    b->reduce_key[q].col = idx;
+  }
+  return SVM_OK;
+}
 
 // Binds a pipeline and resolves its pre_pipeline_id objects.
 svm_status resolve(Ctx* x, const svm_pipeline* p, Bound* b, ObjectPtr* src, std::vector<ObjectPtr>* refs) {
@@ -863,7 +1018,7 @@ svm_status resolve(Ctx* x, const svm_pipeline* p, Bound* b, ObjectPtr* src, std:
                      std::string("no object ") + (p->pre_pipeline_id[i] ? p->pre_pipeline_id[i] : "(null)"));
     refs->push_back(o);
   }
-  return SVM_OK;
+  return resolve_strings(x, b, *src, *refs);
 }
 
 struct BatchItem {
@@ -1386,6 +1541,7 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
     out->has_bulks = true;
     out->bulk0_rows = out->nrows;
     out->source_rows = out->nrows;
+    if ((st = translate_keys(x, it.b, out))) return st;
     x->objects[it.id] = out;
   }
   return SVM_OK;

@@ -65,7 +65,8 @@ class Engine:
 
     # ------------------------------------------------------------ objects
     def put(self, oid: str, columns, on_device: bool = False, nrows: int | None = None):
-        """Store host arrays (int32/int64 numpy) or device pointers as object `oid`.
+        """Store host arrays (int32/int64 numpy, or fixed-width bytes 'S<w>'
+        for String columns of width w) or device pointers as object `oid`.
         A None column is left zeroed (int32; pass nrows when every column is None)."""
         n = len(columns)
         if on_device:
@@ -75,14 +76,21 @@ class Engine:
             keep = None
         else:
             keep = [None if c is None else np.ascontiguousarray(c) for c in columns]
-            types = [capi_type(np.int32 if c is None else c.dtype) for c in keep]
+            types = [int(ValType.String) if c is not None and c.dtype.kind == "S" else
+                     capi_type(np.int32 if c is None else c.dtype) for c in keep]
             lens = {len(c) for c in keep if c is not None}
             if len(lens) > 1:
                 raise ValueError("columns differ in length")
             nrows = lens.pop() if lens else (nrows or 0)
             ptrs = [ctypes.c_void_p(None if c is None else c.ctypes.data) for c in keep]
-        t = (ctypes.c_int * n)(*types)
         pa = (ctypes.c_void_p * n)(*ptrs)
+        if not on_device and any(c is not None and c.dtype.kind == "S" for c in keep):
+            descs = (capi.svm_column_desc * n)(*[
+                capi.svm_column_desc(int(ValType.String), c.dtype.itemsize) if c is not None and c.dtype.kind == "S"
+                else capi.svm_column_desc(t, 8 if t == int(ValType.Int64) else 4) for c, t in zip(keep, types)])
+            self._check(self.lib.svm_object_put_columns(self.h, oid.encode(), n, descs, nrows, pa, 0))
+            return
+        t = (ctypes.c_int * n)(*types)
         self._check(self.lib.svm_object_put(self.h, oid.encode(), n, t, nrows, pa, int(on_device)))
         del keep
 
@@ -119,10 +127,19 @@ class Engine:
         self._check(self.lib.svm_object_types(self.h, oid.encode(), t, nc))
         return list(t)[:nc]
 
+    def columns(self, oid: str) -> list[tuple[int, int]]:
+        """(ValType, val_size) of each column (a String column's width in bytes)."""
+        nc, _ = self.info(oid)
+        d = (capi.svm_column_desc * max(nc, 1))()
+        self._check(self.lib.svm_object_columns(self.h, oid.encode(), d, nc))
+        return [(d[k].type, d[k].val_size) for k in range(nc)]
+
     def read(self, oid: str, col: int, row0: int = 0, n: int | None = None) -> np.ndarray:
+        """Rows of one column: int32 / int64, or 'S<w>' bytes for a String column."""
         _, nr = self.info(oid)
         n = nr - row0 if n is None else n
-        dt = np.int64 if self.types(oid)[col] == ValType.Int64 else np.int32
+        t, w = self.columns(oid)[col]
+        dt = np.dtype(f"S{w}") if t == ValType.String else np.int64 if t == ValType.Int64 else np.int32
         out = np.empty(n, dt)
         self._check(self.lib.svm_object_read(self.h, oid.encode(), col, row0, n,
                                              out.ctypes.data_as(ctypes.c_void_p)))

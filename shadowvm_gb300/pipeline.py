@@ -58,12 +58,14 @@ STR = ValType.String
 
 
 def dim_pipeline(pid: str, source: str, src_schema: ObjectInfo, select: str, predication: str | None,
-                 hash_col_size: int = 40) -> PipelineInfo:
+                 hash_col_size: int = 40, out_cols: list | None = None) -> PipelineInfo:
     """Dimension-side pipeline as the reference drivers write them
     (e.g. example/run_SSB_Q31.cu:11-25): Source -> [Filter] -> Map -> Sink,
-    output = the selected int columns plus the trailing hash-table column."""
+    output = the selected columns (int32, or out_cols' (ValType, val_size)
+    each, e.g. String copies) plus the trailing hash-table column."""
     n = len(str_split(select, ","))
-    out = create_schema([I32] * n + [STR], [4] * n + [hash_col_size])
+    cols = out_cols or [(I32, 4)] * n
+    out = create_schema([t for t, _ in cols] + [STR], [z for _, z in cols] + [hash_col_size])
     t = PipelineTest(pid).add_pre(source)
     t.add_operator(OpType.Source, {"type": "object"}, src_schema)
     if predication:

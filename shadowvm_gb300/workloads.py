@@ -8,6 +8,10 @@ outputs and reducing (example/run_SSB_Q11.cu, run_SSB_Q31.cu).
             GROUP BY (c_nation, s_nation, year) SUM(revenue - supplycost)
   config 3  a batch of 256 queries shaped like configs 0-2 over views of the
             resident 600 M-row config-2 fact table (make_batch)
+  config 5  config 2's query over dimension tables whose city / nation /
+            region are fixed-width String columns: StrCmp region filters,
+            GROUP BY the nation strings (Hash keys), as the reference's string
+            SSB queries are written (java_vRDD/.../SSBHelper.java:176-206)
 
 Every size can be scaled down for tests.  All columns are seeded and
 counter-based (datagen.py), so the fact table is generated on the device by
@@ -29,10 +33,45 @@ FACT_COLS = {
     2: ["orderdate", "quantity", "discount", "extprice", "partkey", "custkey", "suppkey", "revenue",
         "supplycost"],
 }
+FACT_COLS[5] = FACT_COLS[2]
+
+# String widths of config 5's geography columns (bytes, NUL-padded).
+CITY_W, NATION_W, REGION_W = 10, 15, 12
 
 
 def int_schema(n: int) -> ObjectInfo:
     return create_schema([ValType.Int32] * n, [4] * n)
+
+
+def schema_of(cols: list) -> ObjectInfo:
+    """The schema of host columns: int32 / int64, or String of width w for 'S<w>' bytes."""
+    types, sizes = [], []
+    for c in cols:
+        dt = np.asarray(c).dtype
+        if dt.kind == "S":
+            types.append(ValType.String)
+            sizes.append(dt.itemsize)
+        else:
+            types.append(ValType.Int64 if dt == np.int64 else ValType.Int32)
+            sizes.append(dt.itemsize)
+    return create_schema(types, sizes)
+
+
+def geo_strings(table: dict) -> list[np.ndarray]:
+    """City / nation / region codes of a geography table as synthetic
+    fixed-width names of varied lengths (no two share a prefix that StrCmp
+    would take for equality)."""
+    def names(codes, fmt, width):
+        uniq = np.unique(codes)
+        lut = {int(u): fmt(int(u)).encode() for u in uniq}
+        return np.array([lut[int(v)] for v in codes], dtype=f"S{width}")
+    return [names(table["city"], lambda c: f"CT{c:03d}" + "xyz"[: c % 4], CITY_W),
+            names(table["nation"], lambda n: f"NAT{n:02d}-" + "nation"[: n % 7], NATION_W),
+            names(table["region"], lambda r: f"RG{r}-" + "region"[: r + 1], REGION_W)]
+
+
+def region_name(r: int) -> str:
+    return f"RG{r}-" + "region"[: r + 1]
 
 
 @dataclass
@@ -50,6 +89,7 @@ class Workload:
     query: PipelineInfo | None = None
     key_num: int = 0
     metric_num: int = 1
+    device_fact: bool = True                        # the library can generate the fact table
 
     @property
     def fact_cols(self) -> list[str]:
@@ -65,7 +105,10 @@ class Workload:
 
     def fact_bytes_per_row(self) -> int:
         """Algorithmic bytes: 4 per distinct fact column the query reads."""
-        return 4 * {0: 4, 1: 3, 2: 5}[self.config]
+        return 4 * {0: 4, 1: 3, 2: 5, 5: 5}[self.config]
+
+    def dim_schema(self, name: str) -> ObjectInfo:
+        return schema_of(self.dims[name])
 
 
 def make(config: int, *, fact_rows: int | None = None, seed: int = dg.DEFAULT_SEED,
@@ -75,6 +118,9 @@ def make(config: int, *, fact_rows: int | None = None, seed: int = dg.DEFAULT_SE
 
     def dflt(v, d):
         return d if v is None else v
+
+    if config == 6:
+        return make_string_edges(dflt(fact_rows, 50_000), dflt(tuple_per_bulk, 20_000), seed)
 
     if config == 0:
         w = Workload(0, dflt(fact_rows, 6_000_000), dflt(tuple_per_bulk, 2_000_000), seed)
@@ -119,6 +165,30 @@ def make(config: int, *, fact_rows: int | None = None, seed: int = dg.DEFAULT_SE
             dim_pipeline("q2_supp", "supplier", int_schema(4), "$(0.0),$(0.2)", f"$(0.3)=={r2}"),
         ]
         w.query = fact_pipeline("q2", "lineorder", w.fact_schema(), ["q2_date", "q2_cust", "q2_supp"],
+                                [("$(0.0)", "$(1.0)"), ("$(0.5)", "$(2.0)"), ("$(0.6)", "$(3.0)")],
+                                "$(2.1),$(3.1),$(1.1)", "$(0.7)-$(0.8)")
+        w.key_num = 3
+    elif config == 5:
+        w = Workload(5, dflt(fact_rows, 600_000_000), dflt(tuple_per_bulk, 3_000_000), seed,
+                     n_part=dflt(n_part, 1_400_000), n_cust=dflt(n_cust, 3_000_000),
+                     n_supp=dflt(n_supp, 200_000))
+        r, r2, y = dg.draw(qs, 5, 0, 4), dg.draw(qs, 6, 0, 4), dg.draw(qs, 7, 1992, 1996)
+        w.params = {"c_region": region_name(r), "s_region": region_name(r2), "year_lo": y}
+        dt = dg.date_table()
+        ct = dg.customer_table(w.n_cust, seed)
+        st = dg.supplier_table(w.n_supp, seed)
+        w.dims = {"date": [dt["datekey"], dt["year"], dt["month"]],
+                  "customer": [ct["key"]] + geo_strings(ct),
+                  "supplier": [st["key"]] + geo_strings(st)}
+        nat = [(ValType.Int32, 4), (ValType.String, NATION_W)]
+        w.dim_pipelines = [
+            dim_pipeline("q5_date", "date", int_schema(3), "$(0.0),$(0.1)", f"$(0.1)>={y} && $(0.1)<={y + 2}"),
+            dim_pipeline("q5_cust", "customer", w.dim_schema("customer"), "$(0.0),$(0.2)",
+                         f'StrCmp($(0.3),"{region_name(r)}",{REGION_W})==0', out_cols=nat),
+            dim_pipeline("q5_supp", "supplier", w.dim_schema("supplier"), "$(0.0),$(0.2)",
+                         f'StrCmp($(0.3),"{region_name(r2)}",{REGION_W})==0', out_cols=nat),
+        ]
+        w.query = fact_pipeline("q5", "lineorder", w.fact_schema(), ["q5_date", "q5_cust", "q5_supp"],
                                 [("$(0.0)", "$(1.0)"), ("$(0.5)", "$(2.0)"), ("$(0.6)", "$(3.0)")],
                                 "$(2.1),$(3.1),$(1.1)", "$(0.7)-$(0.8)")
         w.key_num = 3
@@ -282,7 +352,7 @@ def load_engine(engine, w: Workload, fact_id: str = "lineorder", generate_on_dev
     """Dimensions from host arrays; the fact table generated on the device."""
     for name, cols in w.dims.items():
         engine.put(name, cols)
-    if generate_on_device:
+    if generate_on_device and w.device_fact:
         gen_fact_on_device(engine, w, fact_id, row0)
     else:
         engine.put(fact_id, w.fact_host(row0, w.fact_rows))
@@ -317,3 +387,55 @@ def ssb_like_text(rows: int, ncols: int, seed: int, width: int = 10) -> tuple[by
     buf[r, c, width - 1 - ndig[r, c]] = ord("-")
     lines = np.concatenate([buf.reshape(rows, -1), np.full((rows, 1), ord("\n"), np.uint8)], axis=1)
     return lines.tobytes(), [vals[:, k] for k in range(ncols)]
+
+
+# ------------------------------------------------------------------ string edge cases
+TAG_NAMES = [b"", b"AM", b"AMER", b"AMERICAN", b"AMERICA", b"Aa", b"BB", b"ZZZZZZZZ", b"\xe9t\xe9", b"amer",
+             b"AMX", b"A"]
+
+
+@dataclass
+class StringEdgeWorkload(Workload):
+    """String semantics the reference's generated code has, on a small star:
+    tag (key, name S8, group S6) and a fact table (tagkey, mode S5, value).
+
+      q6_tag   Filter StrCmp(name, "AMERICA", 8) == 0 -- true for "", "A",
+               "AM", "AMER", "AMERICA" and "AMERICAN" (StrCmp stops at either
+               NUL, com/cpp/cpu-runtime.hpp:37-45) -- or >= "B", == "Aa", or
+               below "A" (signed chars: "\xe9t\xe9" is, "" is not);
+               Map key, name (S8), group cut to S4 (StrCopy of 4 bytes)
+      q6       Filter StrCmp(mode, "RAIL", 5) != 0 on the fact table; join
+               tag; GROUP BY name, group, mode -- Hash keys, where "Aa" and
+               "BB" collide (seed 31) and merge as in the reference
+    """
+
+    device_fact: bool = False
+
+    def fact_schema(self) -> ObjectInfo:
+        return create_schema([ValType.Int32, ValType.String, ValType.Int32], [4, 5, 4])
+
+    def fact_host(self, row0: int, n: int) -> list[np.ndarray]:
+        tk = dg.uniform(self.seed, 91, 0, len(TAG_NAMES) - 1, row0, n).astype(np.int32)
+        modes = np.array([b"RAIL", b"AIR", b"SHIP", b"TRUCK", b"RAILS", b""], dtype="S5")
+        mode = modes[dg.uniform(self.seed, 92, 0, len(modes) - 1, row0, n)]
+        val = dg.uniform(self.seed, 93, -1000, 100_000, row0, n).astype(np.int32)
+        return [tk, mode, val]
+
+    def fact_bytes_per_row(self) -> int:
+        return 12
+
+
+def make_string_edges(fact_rows: int = 50_000, tuple_per_bulk: int = 20_000, seed: int = dg.DEFAULT_SEED):
+    w = StringEdgeWorkload(6, fact_rows, tuple_per_bulk, seed)
+    # group cut to 4 bytes pairs the tags (k + 1) // 2: "Aa" (5) and "BB" (6) share it
+    groups = [f"G{((k + 1) // 2) % 3}#{((k + 1) // 2) % 2}{k:02d}".encode() for k in range(len(TAG_NAMES))]
+    w.dims = {"tag": [np.arange(len(TAG_NAMES), dtype=np.int32), np.array(TAG_NAMES, dtype="S8"),
+                      np.array(groups, dtype="S6")]}
+    w.dim_pipelines = [dim_pipeline("q6_tag", "tag", w.dim_schema("tag"), "$(0.0),$(0.1),$(0.2)",
+                                    'StrCmp($(0.1),"AMERICA",8)==0 || StrCmp($(0.1),"B",8)>=0 || '
+                                    'StrCmp($(0.1),"Aa",8)==0 || StrCmp($(0.1),"A",8)<0',
+                                    out_cols=[(ValType.Int32, 4), (ValType.String, 8), (ValType.String, 4)])]
+    w.query = fact_pipeline("q6", "lineorder", w.fact_schema(), ["q6_tag"], [("$(0.0)", "$(1.0)")],
+                            "$(1.1),$(1.2),$(0.1)", "$(0.2)", predication='StrCmp($(0.1),"RAIL",5)!=0')
+    w.key_num = 3
+    return w

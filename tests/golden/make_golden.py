@@ -42,6 +42,13 @@ CASES = [
                          n_supp=8_000, qseed=7), True),
     # an empty fact table: no bulk, no result row
     ("c0_empty", 0, dict(fact_rows=0, tuple_per_bulk=100_000), False),
+    # String dimension columns: StrCmp region filters, GROUP BY nation strings (Hash keys)
+    ("c5_small", 5, dict(fact_rows=300_000, tuple_per_bulk=100_000, n_part=20_000, n_cust=60_000,
+                         n_supp=8_000), False),
+    ("c5_q9", 5, dict(fact_rows=200_000, tuple_per_bulk=100_000, n_part=20_000, n_cust=40_000,
+                      n_supp=6_000, qseed=9), False),
+    # StrCmp's NUL rules, a Hash collision, signed chars, a cut Map copy, a String fact column
+    ("c6_edges", 6, dict(fact_rows=50_000, tuple_per_bulk=20_000), False),
 ]
 
 

@@ -124,9 +124,17 @@ def test_errors_are_reported(engine_factory):
     with pytest.raises(SvmError) as e:
         eng.run(fact_pipeline("q", "missing", W.int_schema(2), ["dd"], [("$(0.0)", "$(1.0)")], "", "$(0.1)"))
     assert e.value.status == capi.E_NOT_FOUND
-    with pytest.raises(SvmError) as e:
+    with pytest.raises(SvmError) as e:  # the metric list splits on commas, as the reference's StrSplit
         eng.run(fact_pipeline("q", "f", W.int_schema(2), ["dd"], [("$(0.0)", "$(1.0)")], "",
                               "StrCmp($(0.1),\"x\",1)"))
+    assert e.value.status == capi.E_INVALID_ARG
+    with pytest.raises(SvmError) as e:  # StrCmp of an int column
+        eng.run(fact_pipeline("q", "f", W.int_schema(2), ["dd"], [("$(0.0)", "$(1.0)")], "", "$(0.1)",
+                              predication='StrCmp($(0.1),"x",1)==0'))
+    assert e.value.status == capi.E_UNSUPPORTED
+    with pytest.raises(SvmError) as e:  # a UDF call
+        eng.run(fact_pipeline("q", "f", W.int_schema(2), ["dd"], [("$(0.0)", "$(1.0)")], "", "$(0.1)",
+                              predication="udf($(0.1))==0"))
     assert e.value.status == capi.E_UNSUPPORTED
     with pytest.raises(SvmError) as e:
         eng.run(fact_pipeline("q", "f", W.int_schema(2), ["dd"], [("$(0.0)", "$(1.0)")], "", "100/$(0.1)"))
