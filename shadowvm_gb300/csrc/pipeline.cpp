@@ -467,6 +467,7 @@ struct StarPlan {
   bool empty_filter = false;    // a contradictory filter: no row passes
   bool needs_prog = false;
   std::vector<DimTablePtr> dim_tables;  // per StarParams dim
+  double est_pass = 1.0;        // expected fraction of rows passing every filter step
 };
 
 svm_status plan_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs,
@@ -696,7 +697,11 @@ svm_status plan_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::ve
   });
   if ((int)order.size() > kMaxSteps) return x->fail(SVM_E_UNSUPPORTED, "more than 8 filter steps");
   P.nsteps = (int)order.size();
-  for (size_t s = 0; s < order.size(); s++) P.steps[s] = order[s].step;
+  plan->est_pass = 1.0;
+  for (size_t s = 0; s < order.size(); s++) {
+    P.steps[s] = order[s].step;
+    plan->est_pass *= order[s].pass;
+  }
   auto operand_of = [&](const ColRef& r, Operand* o) -> bool {
     if (r.obj == 0) {
       *o = Operand{(int8_t)col_slot(r.col), -1};
@@ -956,6 +961,13 @@ svm_status ensure_rank_col(Ctx* x, const ObjectPtr& o, int c, int* idx) {
 // their hash-rank columns (b->key_hash keeps the way back); String join keys
 // and any other use of a String column are unsupported.
 svm_status resolve_strings(Ctx* x, Bound* b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs) {
+  // Nothing to do without String columns or StrCmp (no parsing on the common path).
+  bool any = !src->strs.empty();
+  for (const ObjectPtr& r : refs) any |= !r->strs.empty();
+  for (const auto* v : {&b->filter_exp, &b->metric_exp, &b->select_exp})
+    for (const std::string& t : *v) any |= t.find("StrCmp") != std::string::npos;
+  b->key_hash.assign(b->reduce_key.size(), {});
+  if (!any) return SVM_OK;
   auto obj_of = [&](int k) -> ObjectPtr {
     return k == 0 ? src : (k >= 1 && k <= (int)refs.size() ? refs[k - 1] : nullptr);
   };
@@ -1394,6 +1406,14 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
     mqs[i] = M;
   }
   const int nmerged = (int)order.size();
+  // Consumer warps claim a tile's queries in descriptor order and wait for
+  // the last at the tile's end: the most aggregation work first (longest
+  // processing time first) keeps that tail short.
+  std::stable_sort(order.begin(), order.end(), [&](int a, int z) {
+    const StarPlan& pa = items[a].plan;
+    const StarPlan& pz = items[z].plan;
+    return pa.est_pass * (pa.nkeys + pa.nmet + 1) > pz.est_pass * (pz.nkeys + pz.nmet + 1);
+  });
   order.insert(order.end(), legacy.begin(), legacy.end());
   svm_status st;
   if (nmerged)
