@@ -117,6 +117,27 @@ def test_gpu_loader_device_text_at_every_alignment(engine_factory):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cd,rd", [(" ", "\n"), (",", ";"), ("\t", "\n"), ("5", "\n"), ("-", "|")])
+def test_gpu_loader_other_delimiters(engine_factory, cd, rd):
+    """Delimiters that can be part of a number or of whitespace (space, tab,
+    a digit, a sign): the field walks must stop at the field's end."""
+    eng = engine_factory()
+    rng = random.Random(ord(cd) * 31 + ord(rd))
+    lines = []
+    for _ in range(3000):
+        fields = [" " * rng.randint(0, 3) + rng.choice(["", "-", "+"]) + str(rng.randint(0, 10 ** rng.randint(1, 12)))
+                  for _ in range(rng.randint(0, 6))]
+        lines.append(cd.join(fields) + (cd if rng.random() < 0.7 else ""))
+    text = (rd.join(lines) + rd).encode()
+    types = [I32, I64, I32, I64]
+    n = eng.load_text("d", text, types, col_delim=cd, row_delim=rd)
+    en, ecols = oracle.load_text(text, types, cd, rd)
+    assert n == en
+    for k in range(len(types)):
+        np.testing.assert_array_equal(eng.read("d", k), ecols[k], err_msg=f"column {k}")
+
+
+@pytest.mark.gpu
 def test_gpu_loader_edges(engine_factory):
     eng = engine_factory()
     for text in [b"", b"\n", b"1|2|", b"1|2|\n", b"|||\n||\n", b"5|" * 100 + b"\n",
