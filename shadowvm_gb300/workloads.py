@@ -57,21 +57,28 @@ def schema_of(cols: list) -> ObjectInfo:
     return create_schema(types, sizes)
 
 
+def city_name(c: int) -> str:
+    return f"CT{c:03d}" + "xyz"[: c % 4]
+
+
+def nation_name(n: int) -> str:
+    return f"NAT{n:02d}-" + "nation"[: n % 7]
+
+
+def region_name(r: int) -> str:
+    return f"RG{r}-" + "region"[: r + 1]
+
+
 def geo_strings(table: dict) -> list[np.ndarray]:
     """City / nation / region codes of a geography table as synthetic
     fixed-width names of varied lengths (no two share a prefix that StrCmp
     would take for equality)."""
     def names(codes, fmt, width):
         uniq = np.unique(codes)
-        lut = {int(u): fmt(int(u)).encode() for u in uniq}
-        return np.array([lut[int(v)] for v in codes], dtype=f"S{width}")
-    return [names(table["city"], lambda c: f"CT{c:03d}" + "xyz"[: c % 4], CITY_W),
-            names(table["nation"], lambda n: f"NAT{n:02d}-" + "nation"[: n % 7], NATION_W),
-            names(table["region"], lambda r: f"RG{r}-" + "region"[: r + 1], REGION_W)]
-
-
-def region_name(r: int) -> str:
-    return f"RG{r}-" + "region"[: r + 1]
+        lut = np.array([fmt(int(u)).encode() for u in uniq], dtype=f"S{width}")
+        return lut[np.searchsorted(uniq, codes)]
+    return [names(table["city"], city_name, CITY_W), names(table["nation"], nation_name, NATION_W),
+            names(table["region"], region_name, REGION_W)]
 
 
 @dataclass
