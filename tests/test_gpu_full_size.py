@@ -63,3 +63,29 @@ def test_full_size_star_query_properties(engine_factory):
     order = np.lexsort(expect.T[::-1])
     np.testing.assert_array_equal(k5, expect[order].astype(np.int32))
     np.testing.assert_array_equal(s5, sums[order])
+
+
+def test_full_size_batch_mix_equals_single_launches(engine_factory):
+    """The 256-query mix over the 600 M-row table: one svm_run_batch equals
+    one svm_run_pipeline per query, bit for bit."""
+    bw = W.make_batch(256)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, batch_policy="always")
+    W.load_batch(eng, bw)
+    eng.run_batch([q.pipe for q in bw.queries])
+    batched = {q.pipe.id: eng.result(q.pipe.id, q.key_num) for q in bw.queries}
+    for q in bw.queries:
+        eng.run(q.pipe)
+        k, s = eng.result(q.pipe.id, q.key_num)
+        np.testing.assert_array_equal(k, batched[q.pipe.id][0], err_msg=q.pipe.id)
+        np.testing.assert_array_equal(s, batched[q.pipe.id][1], err_msg=q.pipe.id)
+
+
+def test_full_size_text_loader_round_trip(engine_factory):
+    """1 GB of SSB-like text (10 M lines of 9 fields) loads into exactly the
+    values it was printed from."""
+    text, cols = W.ssb_like_text(10_000_000, 9, 21)
+    assert len(text) == 1_000_000_000
+    eng = engine_factory()
+    assert eng.load_text("big", text, [2] * 9) == 10_000_000
+    for k in range(9):
+        np.testing.assert_array_equal(eng.read("big", k), cols[k].astype(np.int32), err_msg=f"column {k}")
