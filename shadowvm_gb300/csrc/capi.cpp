@@ -159,6 +159,11 @@ svm_status Ctx::scratch_take(size_t bytes, void** out) {
   return SVM_OK;
 }
 
+void Ctx::purge_rank_cache() {
+  for (auto it = rank_cache.begin(); it != rank_cache.end();)
+    it = it->second.codes.use_count() == 1 ? rank_cache.erase(it) : std::next(it);
+}
+
 svm_status Ctx::column_stats(const ObjectPtr& o, int c, ColStats* out) {
   if (o->stats.size() < o->types.size()) o->stats.resize(o->types.size());
   if (!o->stats[c].valid) {
@@ -382,6 +387,7 @@ svm_status svm_object_put_columns(svm_ctx* c, const char* id, int ncols, const s
   cudaError_t e = cudaStreamSynchronize(x->stream);
   if (e) return x->cuda_fail(e, "object upload");
   x->objects[id] = o;
+  x->purge_rank_cache();
   return SVM_OK;
 }
 
@@ -614,6 +620,7 @@ svm_status svm_object_drop(svm_ctx* c, const char* id) {
   if (it == x->objects.end()) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
   cudaStreamSynchronize(x->stream);
   x->objects.erase(it);
+  x->purge_rank_cache();
   // Tables built over the dropped object are keyed by its version; drop them
   // too, with the merged probe tables made from them.
   std::vector<const svm::DimTable*> gone;

@@ -9,6 +9,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/svm_capi.h"
@@ -136,6 +137,15 @@ struct Ctx {
   std::map<std::string, DimTablePtr> dim_cache;
   std::map<std::string, MergedTable> merged_cache;
   unsigned long long merged_stamp = 0;
+  // Hash-rank columns of String code columns, one per (code storage,
+  // dictionary, width), over the storage's whole extent so that every view
+  // of an object shares it; holds the code storage alive (and unreusable).
+  struct RankCol {
+    DevBufPtr codes, ranks;
+    std::vector<int32_t> hash_of_rank;
+  };
+  std::map<std::tuple<const void*, const void*, int>, RankCol> rank_cache;
+  void purge_rank_cache();  // entries whose code storage no object uses any more
   int* d_error = nullptr;                     // device error word
   // Grow-only scratch arena, carved per operation.
   DevBufPtr scratch;

@@ -920,38 +920,50 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
 namespace {
 
 // The derived column of object o's String column c holding each row's rank
-// among the column's distinct Hash values (built once per object).
+// among the Hash values of the codes its storage holds.  It is computed once
+// per code storage over the storage's whole extent (its zeroed padding rows
+// hold code 0), so views of an object share it and a batched union scan over
+// several views' ranges stays inside it.
 svm_status ensure_rank_col(Ctx* x, const ObjectPtr& o, int c, int* idx) {
   StrCol& sc = o->strs.at(c);
   if (sc.rank_col >= 0) {
     *idx = sc.rank_col;
     return SVM_OK;
   }
-  // The codes the column holds, then ranks over their hashes only.
-  const uint32_t D = sc.dict->count;
-  std::vector<uint32_t> present(D, 0);
-  DevBufPtr flags, lut, col;
-  svm_status st;
-  if ((st = x->alloc(4ull * D + 4, &flags, true))) return st;
-  cudaError_t e = launch_mark_codes((const int32_t*)o->col(c), o->nrows, (uint32_t*)flags->p, x->stream);
-  if (!e && D) e = cudaMemcpyAsync(present.data(), flags->p, 4ull * D, cudaMemcpyDeviceToHost, x->stream);
-  if (!e) e = cudaStreamSynchronize(x->stream);
-  if (e) return x->cuda_fail(e, "string key codes");
-  std::vector<int32_t> rank_of_code, hash_of_rank;
-  hash_ranks(*sc.dict, sc.width, present, &rank_of_code, &hash_of_rank);
-  const unsigned long long rows = o->row0 + o->nrows, padded = (rows + 63) / 64 * 64 + 64;
-  if ((st = x->alloc(4 * rank_of_code.size() + 4, &lut)) || (st = x->alloc(4 * padded, &col, true))) return st;
-  e = cudaMemcpyAsync(lut->p, rank_of_code.data(), 4 * rank_of_code.size(), cudaMemcpyHostToDevice, x->stream);
-  if (!e) e = launch_lut_gather((const int32_t*)o->col(c), o->nrows, (const int32_t*)lut->p,
-                                (int32_t*)col->p + o->row0, x->stream);
-  if (e) return x->cuda_fail(e, "string key ranks");
-  if ((st = sync_and_check(x, "string key ranks"))) return st;
+  const DevBufPtr& codes = o->storage[c];
+  const auto key = std::make_tuple((const void*)codes.get(), (const void*)sc.dict.get(), sc.width);
+  auto it = x->rank_cache.find(key);
+  if (it == x->rank_cache.end()) {
+    const unsigned long long rows = codes->bytes / 4;
+    const uint32_t D = sc.dict->count;
+    std::vector<uint32_t> present(D, 0);
+    DevBufPtr flags, lut, ranks;
+    svm_status st;
+    if ((st = x->alloc(4ull * D + 4, &flags, true))) return st;
+    cudaError_t e = launch_mark_codes((const int32_t*)codes->p, rows, (uint32_t*)flags->p, x->stream);
+    if (!e && D) e = cudaMemcpyAsync(present.data(), flags->p, 4ull * D, cudaMemcpyDeviceToHost, x->stream);
+    if (!e) e = cudaStreamSynchronize(x->stream);
+    if (e) return x->cuda_fail(e, "string key codes");
+    Ctx::RankCol rc;
+    std::vector<int32_t> rank_of_code;
+    hash_ranks(*sc.dict, sc.width, present, &rank_of_code, &rc.hash_of_rank);
+    if ((st = x->alloc(4 * rank_of_code.size() + 4, &lut)) || (st = x->alloc(4 * rows, &ranks, true))) return st;
+    e = cudaMemcpyAsync(lut->p, rank_of_code.data(), 4 * rank_of_code.size(), cudaMemcpyHostToDevice, x->stream);
+    if (!e) e = launch_lut_gather((const int32_t*)codes->p, rows, (const int32_t*)lut->p, (int32_t*)ranks->p,
+                                  x->stream);
+    if (e) return x->cuda_fail(e, "string key ranks");
+    if ((st = sync_and_check(x, "string key ranks"))) return st;
+    rc.codes = codes;
+    rc.ranks = ranks;
+    it = x->rank_cache.emplace(key, std::move(rc)).first;
+  }
   o->types.push_back(SVM_INT32);
-  o->storage.push_back(col);
+  o->storage.push_back(it->second.ranks);
   if (o->stats.size() < o->types.size()) o->stats.resize(o->types.size());
-  o->stats.back() = ColStats{true, 0, hash_of_rank.empty() ? 0 : (int32_t)hash_of_rank.size() - 1};
+  const int32_t h = (int32_t)it->second.hash_of_rank.size();
+  o->stats.back() = ColStats{true, 0, h > 0 ? h - 1 : 0};
   sc.rank_col = (int)o->types.size() - 1;
-  sc.rank_hash = std::move(hash_of_rank);
+  sc.rank_hash = it->second.hash_of_rank;
   *idx = sc.rank_col;
   return SVM_OK;
 }

@@ -125,3 +125,31 @@ def test_string_uses_outside_the_grammar_are_refused(engine_factory):
     # accepted: the escaped-quote form of the Java DSL
     eng.run(dim_pipeline("esc", "u", src, "$(0.0)", 'StrCmp($(0.1),\\"abd\\",3)==0'))
     np.testing.assert_array_equal(eng.read("esc", 0), np.arange(1, 100, 2, dtype=np.int32))
+
+
+def test_string_fact_keys_over_views_in_one_batch(engine_factory):
+    """GROUP BY a String column of the fact table over two views with
+    different row ranges, in one batched launch: the union scan covers both
+    ranges, and the views share one hash-rank column spanning the table."""
+    rng = np.random.default_rng(8)
+    n = 1_000_000
+    modes = np.array([b"RAIL", b"AIR", b"SHIP", b"", b"TRUCK", b"Aa", b"BB"], dtype="S5")
+    fact = [rng.integers(0, 50, n, dtype=np.int32), modes[rng.integers(0, len(modes), n)],
+            rng.integers(-1000, 1000, n, dtype=np.int32)]
+    dim = [np.arange(50, dtype=np.int32), np.arange(50, dtype=np.int32) % 7]
+    eng = engine_factory(tuple_per_bulk=2_000_000, batch_policy="always")
+    eng.put("f", fact)
+    eng.put("d", dim)
+    eng.run(dim_pipeline("dd", "d", W.int_schema(2), "$(0.0),$(0.1)", "$(0.1) < 5"))
+    eng.view("v1", "f", 0, 300_000)
+    eng.view("v2", "f", 500_000, 500_000)
+    src = create_schema([I32, S, I32], [4, 5, 4])
+    qs = [fact_pipeline(f"m{v}", f"v{v}", src, ["dd"], [("$(0.0)", "$(1.0)")], "$(0.1),$(1.1)", "$(0.2)")
+          for v in (1, 2)]
+    eng.run_batch(qs)
+    dsel = sql_exact.run_select(dim_pipeline("dd", "d", W.int_schema(2), "$(0.0),$(0.1)", "$(0.1) < 5"), dim)
+    for q, (a, b) in zip(qs, [(0, 300_000), (500_000, 1_000_000)]):
+        k, s = eng.result(q.id, 2)
+        ek, es = sql_exact.run_reduce(q, [c[a:b] for c in fact], [dsel])
+        np.testing.assert_array_equal(k, ek)
+        np.testing.assert_array_equal(s, es)
