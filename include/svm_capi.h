@@ -80,6 +80,9 @@ typedef struct svm_config {
   int batch_policy;                  /* svm_run_batch: SVM_BATCH_AUTO (default) picks the cheaper
                                         of one shared launch and per-query launches by a cost
                                         model; SVM_BATCH_ALWAYS / SVM_BATCH_NEVER force one */
+  int autotune;                      /* 1 (default): the first run of each query shape times the
+                                        fitting launch configurations (ring depth, shared-memory
+                                        table placement) and keeps the fastest; 0: a fixed rule */
 } svm_config;
 
 enum { SVM_BATCH_AUTO = 0, SVM_BATCH_ALWAYS = 1, SVM_BATCH_NEVER = 2 };

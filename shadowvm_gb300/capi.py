@@ -25,7 +25,8 @@ K_STAR, K_SELECT, K_BUILD, K_FINALIZE, K_BATCH, K_OTHER, K_LOAD, K_COUNT = range
 class svm_config(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_ulonglong),
                 ("tuple_per_bulk", ctypes.c_ulonglong), ("join_mode", ctypes.c_int),
-                ("hash_char_signed", ctypes.c_int), ("batch_policy", ctypes.c_int)]
+                ("hash_char_signed", ctypes.c_int), ("batch_policy", ctypes.c_int),
+                ("autotune", ctypes.c_int)]
 
 
 class svm_arg(ctypes.Structure):

@@ -246,6 +246,7 @@ void svm_config_default(svm_config* cfg) {
   cfg->join_mode = SVM_JOIN_REF_COMPAT;
   cfg->hash_char_signed = 1;
   cfg->batch_policy = SVM_BATCH_AUTO;
+  cfg->autotune = 1;
 }
 
 svm_status svm_init(const svm_config* cfg, svm_ctx** out) {

@@ -792,6 +792,34 @@ svm_status plan_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::ve
   return SVM_OK;
 }
 
+// The shape a star launch is tuned for: columns, steps (kind, table layout,
+// placement, entry width), dimensions, aggregation, and the orders of
+// magnitude of the group count and the rows scanned.
+std::string star_shape_key(const StarParams& P) {
+  auto lg = [](unsigned long long v) {
+    int b = 0;
+    while (v > 1) {
+      v >>= 1;
+      b++;
+    }
+    return b;
+  };
+  std::string k = std::to_string(P.ncols) + ":" + std::to_string(P.ndims) + ":" + std::to_string(P.agg) + ":" +
+                  std::to_string(P.nkeys) + ":" + std::to_string(P.nmetrics) + ":" + std::to_string(P.npost) + ":" +
+                  std::to_string(lg(P.ngroups)) + ":" +
+                  std::to_string(lg((unsigned long long)(P.row_end - P.row_begin) + 1)) + ":" +
+                  std::to_string(P.agg_words) + "|";
+  for (int i = 0; i < P.nsteps; i++) {
+    const Step& st = P.steps[i];
+    const DimDesc* D = st.kind == STEP_PROBE ? &P.dims[st.dim] : nullptr;
+    k += std::to_string(st.kind) + (D ? "," + std::to_string(D->layout) + "," +
+                                            std::to_string(D->smem_word_off >= 0) + "," +
+                                            std::to_string(D->entry_bits) + "," + std::to_string(lg(D->span))
+                                      : std::string()) + ";";
+  }
+  return k;
+}
+
 // Hash-rank keys back to the reference's Hash values (ranks order like the
 // hashes, so the rows stay sorted by key).
 svm_status translate_keys(Ctx* x, const Bound& b, const ObjectPtr& out) {
@@ -845,22 +873,77 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   if (e) return x->cuda_fail(e, "cudaMemsetAsync");
   if (empty) P.row_end = P.row_begin;  // a contradictory filter: no row can pass
 
-  // Ring depth: the most resident blocks per SM, then the deepest ring.
-  int best_blocks = 0, best_st = 0;
-  for (int nst = kStages; nst >= 2; nst--) {
-    P.nstages = nst;
-    size_t sm = star_smem_bytes(P);
-    int blocks = sm <= 200 * 1024 ? star_blocks_per_sm(P, sm) : 0;
-    if (blocks > best_blocks) {
-      best_blocks = blocks;
-      best_st = nst;
+  // Launch configuration: ring depth x whether the small dimension tables are
+  // staged in shared memory.  The rule: the most resident blocks per SM, then
+  // the deepest ring, tables staged.  With autotuning, every fitting
+  // candidate is timed once per plan shape on the query itself (each trial
+  // starts from zeroed slots, so the result is the same whichever wins).
+  struct Cand {
+    int nst;
+    bool staged;
+    int blocks;
+  };
+  std::vector<int> staged_off(P.ndims);
+  for (int d = 0; d < P.ndims; d++) staged_off[d] = P.dims[d].smem_word_off;
+  const int staged_words = P.smem_table_words;
+  bool any_staged = false;
+  for (int d = 0; d < P.ndims; d++) any_staged |= staged_off[d] >= 0;
+  auto configure = [&](const Cand& c) {
+    P.nstages = c.nst;
+    for (int d = 0; d < P.ndims; d++) P.dims[d].smem_word_off = c.staged ? staged_off[d] : -1;
+    P.smem_table_words = c.staged ? staged_words : 0;
+    flatten_plan(P);
+  };
+  std::vector<Cand> cands;
+  for (int staged = 1; staged >= (any_staged ? 0 : 1); staged--)
+    for (int nst = kStages; nst >= 2; nst--) {
+      Cand c{nst, staged != 0, 0};
+      configure(c);
+      const size_t sm = star_smem_bytes(P);
+      c.blocks = sm <= 200 * 1024 ? star_blocks_per_sm(P, sm) : 0;
+      if (c.blocks > 0) cands.push_back(c);
+    }
+  if (cands.empty()) return x->fail(SVM_E_UNSUPPORTED, "shared-memory plan too large");
+  Cand pick = cands[0];
+  for (const Cand& c : cands)
+    if (c.staged && (c.blocks > pick.blocks || !pick.staged)) pick = c;
+  cudaEvent_t ev;
+  if (x->cfg.autotune && cands.size() > 1) {
+    const std::string key = star_shape_key(P);
+    auto hit = x->star_tune.find(key);
+    if (hit != x->star_tune.end()) {
+      pick = Cand{hit->second.first, hit->second.second, 1};
+    } else {
+      cudaEvent_t t0, t1;
+      cudaEventCreate(&t0);
+      cudaEventCreate(&t1);
+      float best = 0.f;
+      for (const Cand& c : cands) {
+        configure(c);
+        const size_t sm = star_smem_bytes(P);
+        if (!e) e = cudaMemsetAsync(sums, 0, agg_bytes, x->stream);
+        if (!e) e = cudaEventRecord(t0, x->stream);
+        if (!e) e = launch_star(P, star_grid_size(P, sm), star_block_size(), sm, x->stream);
+        if (!e) e = cudaEventRecord(t1, x->stream);
+        if (!e) e = cudaEventSynchronize(t1);
+        float ms = 0.f;
+        if (!e) e = cudaEventElapsedTime(&ms, t0, t1);
+        if (e) break;
+        if (best == 0.f || ms < best) {
+          best = ms;
+          pick = c;
+        }
+      }
+      cudaEventDestroy(t0);
+      cudaEventDestroy(t1);
+      if (e) return x->cuda_fail(e, "star kernel tuning");
+      x->star_tune[key] = {pick.nst, pick.staged};
+      if ((e = cudaMemsetAsync(sums, 0, agg_bytes, x->stream))) return x->cuda_fail(e, "cudaMemsetAsync");
     }
   }
-  if (best_blocks == 0) return x->fail(SVM_E_UNSUPPORTED, "shared-memory plan too large");
-  P.nstages = best_st;
+  configure(pick);
   size_t smem = star_smem_bytes(P);
   int grid = star_grid_size(P, smem);
-  cudaEvent_t ev;
   x->prof_begin(SVM_K_STAR, &ev);
   e = launch_star(P, grid, star_block_size(), smem, x->stream);
   x->prof_end(SVM_K_STAR, ev);

@@ -16,7 +16,8 @@ class Engine:
     """One data-plane context on one GPU."""
 
     def __init__(self, device: int = 0, tuple_per_bulk: int = 2_000_000, join_mode: str = "ref_compat",
-                 hbm_budget_bytes: int = 0, hash_char_signed: bool = True, batch_policy: str = "auto"):
+                 hbm_budget_bytes: int = 0, hash_char_signed: bool = True, batch_policy: str = "auto",
+                 autotune: bool = True):
         self.lib = capi.load()
         cfg = capi.svm_config()
         self.lib.svm_config_default(ctypes.byref(cfg))
@@ -26,6 +27,7 @@ class Engine:
         cfg.hbm_budget_bytes = hbm_budget_bytes
         cfg.hash_char_signed = int(hash_char_signed)
         cfg.batch_policy = {"auto": 0, "always": 1, "never": 2}[batch_policy]
+        cfg.autotune = int(autotune)
         h = ctypes.c_void_p()
         st = self.lib.svm_init(ctypes.byref(cfg), ctypes.byref(h))
         if st != capi.OK:

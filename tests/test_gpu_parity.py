@@ -153,3 +153,23 @@ def test_empty_dimension_and_no_passing_rows(engine_factory):
     w0.query.workflow[1].args["predication"] = "$(0.1)<0"
     keys, sums = run_gpu(engine_factory, w0)
     assert sums.tolist() == [[0]]
+
+
+@pytest.mark.parametrize("config", [0, 1, 2, 5])
+def test_autotuned_launch_equals_fixed_rule(engine_factory, config):
+    """The launch tuner times several configurations on the query itself;
+    whichever it keeps, the result equals the fixed rule's, first run and
+    cached run alike."""
+    w = W.make(config, fact_rows=400_000, tuple_per_bulk=200_000, n_part=20_000, n_cust=50_000, n_supp=6_000)
+    res = []
+    for tune in (True, False):
+        eng = engine_factory(tuple_per_bulk=w.tuple_per_bulk, autotune=tune)
+        W.load_engine(eng, w)
+        first = W.run_engine(eng, w)
+        eng.run(w.query)
+        again = eng.result(w.query.id, w.key_num)
+        np.testing.assert_array_equal(first[0], again[0])
+        np.testing.assert_array_equal(first[1], again[1])
+        res.append(first)
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    np.testing.assert_array_equal(res[0][1], res[1][1])
