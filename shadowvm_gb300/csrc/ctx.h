@@ -145,8 +145,9 @@ struct Ctx {
     std::vector<int32_t> hash_of_rank;
   };
   std::map<std::tuple<const void*, const void*, int>, RankCol> rank_cache;
-  // Tuned star launches: plan shape -> (ring depth, tables staged in shared memory).
-  std::map<std::string, std::pair<int, bool>> star_tune;
+  // Tuned star launches: plan shape -> (ring depth, tables staged in shared
+  // memory, adjacent L2 probes exchanged at this step or -1).
+  std::map<std::string, std::tuple<int, bool, int>> star_tune;
   void purge_rank_cache();  // entries whose code storage no object uses any more
   int* d_error = nullptr;                     // device error word
   // Grow-only scratch arena, carved per operation.

@@ -878,9 +878,12 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   // the deepest ring, tables staged.  With autotuning, every fitting
   // candidate is timed once per plan shape on the query itself (each trial
   // starts from zeroed slots, so the result is the same whichever wins).
+  // With tuning, also the order of two adjacent probes of tables kept in L2
+  // (filters commute; their relative cost depends on the tables' sizes).
   struct Cand {
     int nst;
     bool staged;
+    int swap;  // >= 0: steps swap and swap + 1 exchanged
     int blocks;
   };
   std::vector<int> staged_off(P.ndims);
@@ -888,31 +891,43 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   const int staged_words = P.smem_table_words;
   bool any_staged = false;
   for (int d = 0; d < P.ndims; d++) any_staged |= staged_off[d] >= 0;
+  const std::vector<Step> steps0(P.steps, P.steps + P.nsteps);
+  const std::string shape = x->cfg.autotune ? star_shape_key(P) : std::string();  // as planned
   auto configure = [&](const Cand& c) {
     P.nstages = c.nst;
     for (int d = 0; d < P.ndims; d++) P.dims[d].smem_word_off = c.staged ? staged_off[d] : -1;
     P.smem_table_words = c.staged ? staged_words : 0;
+    for (int k = 0; k < P.nsteps; k++) P.steps[k] = steps0[k];
+    if (c.swap >= 0) std::swap(P.steps[c.swap], P.steps[c.swap + 1]);
     flatten_plan(P);
   };
-  std::vector<Cand> cands;
-  for (int staged = 1; staged >= (any_staged ? 0 : 1); staged--)
-    for (int nst = kStages; nst >= 2; nst--) {
-      Cand c{nst, staged != 0, 0};
-      configure(c);
-      const size_t sm = star_smem_bytes(P);
-      c.blocks = sm <= 200 * 1024 ? star_blocks_per_sm(P, sm) : 0;
-      if (c.blocks > 0) cands.push_back(c);
+  std::vector<int> swaps = {-1};
+  if (x->cfg.autotune)
+    for (int k = 0; k + 1 < P.nsteps; k++) {
+      const Step &a = steps0[k], &z = steps0[k + 1];
+      if (a.kind == STEP_PROBE && z.kind == STEP_PROBE && staged_off[a.dim] < 0 && staged_off[z.dim] < 0)
+        swaps.push_back(k);
     }
+  std::vector<Cand> cands;
+  for (int sw : swaps)
+    for (int staged = 1; staged >= (any_staged ? 0 : 1); staged--)
+      for (int nst = kStages; nst >= 2; nst--) {
+        Cand c{nst, staged != 0, sw, 0};
+        configure(c);
+        const size_t sm = star_smem_bytes(P);
+        c.blocks = sm <= 200 * 1024 ? star_blocks_per_sm(P, sm) : 0;
+        if (c.blocks > 0) cands.push_back(c);
+      }
   if (cands.empty()) return x->fail(SVM_E_UNSUPPORTED, "shared-memory plan too large");
   Cand pick = cands[0];
   for (const Cand& c : cands)
-    if (c.staged && (c.blocks > pick.blocks || !pick.staged)) pick = c;
+    if (c.swap < 0 && c.staged && (c.blocks > pick.blocks || !pick.staged)) pick = c;
   cudaEvent_t ev;
   if (x->cfg.autotune && cands.size() > 1) {
-    const std::string key = star_shape_key(P);
+    const std::string& key = shape;
     auto hit = x->star_tune.find(key);
     if (hit != x->star_tune.end()) {
-      pick = Cand{hit->second.first, hit->second.second, 1};
+      pick = Cand{std::get<0>(hit->second), std::get<1>(hit->second), std::get<2>(hit->second), 1};
     } else {
       cudaEvent_t t0, t1;
       cudaEventCreate(&t0);
@@ -937,7 +952,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
       cudaEventDestroy(t0);
       cudaEventDestroy(t1);
       if (e) return x->cuda_fail(e, "star kernel tuning");
-      x->star_tune[key] = {pick.nst, pick.staged};
+      x->star_tune[key] = std::make_tuple(pick.nst, pick.staged, pick.swap);
       if ((e = cudaMemsetAsync(sums, 0, agg_bytes, x->stream))) return x->cuda_fail(e, "cudaMemsetAsync");
     }
   }
