@@ -137,6 +137,14 @@ struct Ctx {
   std::map<std::string, DimTablePtr> dim_cache;
   std::map<std::string, MergedTable> merged_cache;
   unsigned long long merged_stamp = 0;
+  // Dense tables that held another value than a fellow table of their merged
+  // probe group at a key present in both: they keep a payload field of their
+  // own in later merges (entries die with their table).
+  std::map<const DimTable*, std::weak_ptr<DimTable>> no_share;
+  bool share_refused(const DimTablePtr& t) const {
+    auto f = no_share.find(t.get());
+    return f != no_share.end() && f->second.lock() == t;
+  }
   // Hash-rank columns of String code columns, one per (code storage,
   // dictionary, width), over the storage's whole extent so that every view
   // of an object shares it; holds the code storage alive (and unreusable).

@@ -347,17 +347,25 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
       const uint32_t need = tile_queries(qlo, qhi, qg, nq, a0 + t * kTileRows, nullptr, false, lane, lt, &na);
       const int32_t* stage = ring + (size_t)s * ncols * kTileRows;
       uint32_t* mwb = mwbuf + (size_t)b * mw_words;
+      // The next tile's copies.  With three or more stages its slot held
+      // tile i - 2 (or nothing yet), which the consumers released together
+      // with the lookup buffer waited for above, so the copies go out before
+      // this tile's lookups and overlap them; with two stages the slot is
+      // the consumers' current tile, and the copies follow the lookups.
+      const bool early = nst >= 3;
+      auto next_tile = [&]() {
+        if (lane == 0) ok = issue_tile(i + 1);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok && lane == 0) raise_error(B.error, DERR_TIMEOUT);
+      };
+      if (tma && early) next_tile();
       for (uint32_t mm = need; mm; mm &= mm - 1) {
         const ProbeGroup& G = B.probe[__ffs(mm) - 1];
         for (int row = fw * kFillRows + lane; row < (fw + 1) * kFillRows; row += 32)
           fill_issue(G, stage, mwb, row, pol_tab);
       }
       cp_async_arrive(&fill_full[b]);
-      if (tma) {
-        if (lane == 0) ok = issue_tile(i + 1);
-        ok = __shfl_sync(0xffffffffu, ok, 0);
-        if (!ok && lane == 0) raise_error(B.error, DERR_TIMEOUT);
-      }
+      if (tma && !early) next_tile();
     }
     // Every copy issued lands before the block may exit (a tile issued but
     // never waited for exists only after a timeout).
@@ -443,6 +451,8 @@ __global__ void merge_build_kernel(const __grid_constant__ MergeBuild M, uint32_
   for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < M.span;
        k += (unsigned long long)gridDim.x * blockDim.x) {
     uint32_t w[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+    bool have = false;  // the shared field holds a present source's value
+    uint32_t sv = 0u, bad = 0u;
     for (int i = 0; i < M.nsrc; i++) {
       const MergeSrc& S = M.src[i];
       const long long idx = (long long)M.key_min + (long long)k - (long long)S.key_min;
@@ -451,12 +461,24 @@ __global__ void merge_build_kernel(const __grid_constant__ MergeBuild M, uint32_
       uint32_t e = S.words[bit >> 5] >> (bit & 31);
       if (S.entry_bits < 32) e &= (1u << S.entry_bits) - 1u;
       w[0] |= (e & 1u) << S.present_bit;
-      const uint32_t pay = S.pay_bits >= 32 ? e >> 1 : (e >> 1) & ((1u << S.pay_bits) - 1u);
+      uint32_t pay = S.pay_bits >= 32 ? e >> 1 : (e >> 1) & ((1u << S.pay_bits) - 1u);
+      if (S.shared) {
+        // Only a present key's value counts; every present source must agree.
+        if (!(e & 1u)) continue;
+        pay += (uint32_t)S.val_off;
+        if (have) {
+          if (pay != sv) bad |= 1u << i;
+          continue;
+        }
+        have = true;
+        sv = pay;
+      }
 #pragma unroll
       for (int z = 0; z < 8; z++)
         if (z == S.pay_word && S.pay_bits > 0) w[z] |= pay << S.pay_bit;
     }
     for (int z = 0; z < M.words; z++) out[k * M.words + z] = w[z];
+    if (bad) atomicOr(M.conflict, bad);
   }
 }
 

@@ -1190,18 +1190,31 @@ bool batch_is_cheaper(const std::vector<BatchItem>& items) {
 // present bits from bit 0 up; payloads (entry >> 1) go first-fit, widest
 // first, into the top of word 0 and then into words 1..7.  At most
 // kMaxMergedWords words per row and kMaxMergedTables table slots per batch.
+//
+// Tables of a column whose payload is one bit-packed field share one field
+// of the group, wide enough for all their values: the same dimension column
+// filtered differently per query (25 part tables, one per category, carry
+// the same brand) then costs one field instead of one each.  At a key that
+// several of them hold, their values must agree; the merged-table build
+// reports any that does not, and such a table keeps a field of its own.
 struct MergePlan {
   struct Place {
     int group = -1, slot = -1, present_bit = 0, pay_word = 0, pay_bit = 0;
+    bool shared = false;  // the payload sits in the group's shared field
+  };
+  struct Share {
+    int word = 0, bit = 0, bits = 0;  // bits 0: the group has no shared field
+    int32_t base = 0;                 // field = value - base
   };
   std::map<std::pair<int, const DimTable*>, Place> place;  // (union column, table) -> placement
   std::vector<ProbeGroup> groups;
+  std::vector<Share> share;
   std::vector<std::vector<std::pair<DimTablePtr, Place>>> members;
   int nmwords = 0;
   std::vector<int> gtab0;                  // group g owns table slots [gtab0[g], gtab0[g + 1])
 };
 
-void plan_merge(const std::vector<BatchQuery>& qs, const std::vector<BatchItem>& items, MergePlan* mp) {
+void plan_merge(Ctx* x, const std::vector<BatchQuery>& qs, const std::vector<BatchItem>& items, MergePlan* mp) {
   std::vector<int> col_order;
   std::map<int, std::vector<DimTablePtr>> by_col;
   for (size_t i = 0; i < qs.size(); i++)
@@ -1219,6 +1232,21 @@ void plan_merge(const std::vector<BatchQuery>& qs, const std::vector<BatchItem>&
     std::stable_sort(tabs.begin(), tabs.end(), [](const DimTablePtr& a, const DimTablePtr& z) {
       return a->desc.entry_bits > z->desc.entry_bits;
     });
+    auto sharable = [&](const DimTablePtr& T) {
+      const DimDesc& d = T->desc;
+      return d.npay == 1 && d.pay[0].col == nullptr && d.pay[0].bits > 0 && T->live > 0 && !x->share_refused(T);
+    };
+    long long smin = LLONG_MAX, smax = LLONG_MIN;
+    int nshare = 0, own_bits = 0;
+    for (const DimTablePtr& T : tabs)
+      if (sharable(T)) {
+        nshare++;
+        own_bits += T->desc.pay[0].bits;
+        smin = std::min<long long>(smin, T->pay_min[0]);
+        smax = std::max<long long>(smax, T->pay_max[0]);
+      }
+    const int sbits = nshare >= 2 ? ceil_log2((unsigned long long)(smax - smin + 1)) : 0;
+    const bool share = nshare >= 2 && sbits < own_bits && sbits <= 31;
     size_t next = 0;
     while (next < tabs.size() && (int)mp->groups.size() < kMaxProbeGroups) {
       // A group takes the column's next tables while their present bits,
@@ -1226,6 +1254,7 @@ void plan_merge(const std::vector<BatchQuery>& qs, const std::vector<BatchItem>&
       const int reserve = (int)std::min<size_t>(32, tabs.size() - next);
       const int g = (int)mp->groups.size();
       mp->groups.push_back(ProbeGroup{col, 1, 0, 0, 0, nullptr});
+      mp->share.emplace_back();
       mp->members.emplace_back();
       int ntab = 0, low0 = 32;
       std::vector<int> freebits;  // words 1..
@@ -1237,6 +1266,9 @@ void plan_merge(const std::vector<BatchQuery>& qs, const std::vector<BatchItem>&
         int pb = 0;
         for (int f = 0; f < T->desc.npay; f++)
           pb = std::max(pb, (int)T->desc.pay[f].shift + (int)T->desc.pay[f].bits - 1);
+        MergePlan::Share& sh = mp->share[g];
+        const bool shared = share && sharable(T);
+        if (shared) pb = sh.bits ? 0 : sbits;  // the group's shared field, placed by its first table
         const long long tmin = T->desc.key_min, tmax = (long long)T->desc.key_min + T->desc.span - 1;
         const long long nmin = std::min(kmin, tmin), nmax = std::max(kmax, tmax);
         if ((nmax - nmin + 1) * 32ll > (1ll << 30)) break;
@@ -1264,6 +1296,12 @@ void plan_merge(const std::vector<BatchQuery>& qs, const std::vector<BatchItem>&
             pl.pay_bit = 32 - freebits[word - 1];
             freebits[word - 1] -= pb;
           }
+          if (shared) sh = MergePlan::Share{word, pl.pay_bit, sbits, (int32_t)smin};
+        }
+        if (shared) {
+          pl.shared = true;
+          pl.pay_word = sh.word;
+          pl.pay_bit = sh.bit;
         }
         ntab++;
         next++;
@@ -1274,6 +1312,7 @@ void plan_merge(const std::vector<BatchQuery>& qs, const std::vector<BatchItem>&
       }
       if (ntab == 0) {  // the next table alone does not fit: leave it unplaced
         mp->groups.pop_back();
+        mp->share.pop_back();
         mp->members.pop_back();
         next++;
         continue;
@@ -1309,13 +1348,19 @@ void plan_merge(const std::vector<BatchQuery>& qs, const std::vector<BatchItem>&
   mp->nmwords = off;
 }
 
-// The merged table of group g, from the cache or built now.
-svm_status merged_table(Ctx* x, MergePlan* mp, int g) {
+// The merged table of group g, from the cache or built now.  A table built
+// now with a shared field reports its sources' disagreements into
+// `*conflict` (device) and its cache key into `*checked`.
+svm_status merged_table(Ctx* x, MergePlan* mp, int g, unsigned int* conflict, std::string* checked) {
   ProbeGroup& G = mp->groups[g];
+  const MergePlan::Share& sh = mp->share[g];
   std::string key = std::to_string(G.key_min) + ":" + std::to_string(G.span) + ":" + std::to_string(G.words);
-  for (auto& m : mp->members[g])
+  for (auto& m : mp->members[g]) {
     key += "|" + std::to_string((uintptr_t)m.first.get()) + "@" + std::to_string(m.second.present_bit) + "." +
            std::to_string(m.second.pay_word) + "." + std::to_string(m.second.pay_bit);
+    if (m.second.shared) key += "s" + std::to_string(sh.bits) + "." + std::to_string(sh.base);
+  }
+  checked->clear();
   auto it = x->merged_cache.find(key);
   if (it == x->merged_cache.end()) {
     if (x->merged_cache.size() >= 64) {  // evict the least recently used
@@ -1333,13 +1378,17 @@ svm_status merged_table(Ctx* x, MergePlan* mp, int g) {
       mb.key_min = G.key_min;
       mb.span = G.span;
       mb.words = G.words;
+      mb.conflict = conflict;
       for (size_t i = b0; i < mp->members[g].size() && mb.nsrc < kMaxMergeSrcs; i++) {
         const auto& m = mp->members[g][i];
         const DimDesc& d = m.first->desc;
         int pb = 0;
         for (int f = 0; f < d.npay; f++) pb = std::max(pb, (int)d.pay[f].shift + (int)d.pay[f].bits - 1);
-        mb.src[mb.nsrc++] = MergeSrc{d.words,   d.key_min, d.span, d.entry_bits, m.second.present_bit,
-                                     m.second.pay_word, m.second.pay_bit, pb};
+        const int32_t off = m.second.shared ? (int32_t)((uint32_t)d.pay[0].min - (uint32_t)sh.base) : 0;
+        mb.src[mb.nsrc++] = MergeSrc{d.words,          d.key_min,          d.span, d.entry_bits,
+                                     m.second.present_bit, m.second.pay_word, m.second.pay_bit, pb,
+                                     m.second.shared ? 1 : 0, off};
+        if (m.second.shared) *checked = key;
         mt.srcs.push_back(m.first);
       }
       if (b0 > 0) return x->fail(SVM_E_UNSUPPORTED, "more than 32 tables in one merged probe group");
@@ -1404,7 +1453,11 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
 
   // ---- merged probe groups, and the queries they cover
   MergePlan mp;
-  plan_merge(qs, items, &mp);
+  std::vector<int> order;
+  std::vector<MQuery> mqs;
+  std::vector<const int32_t*> gcols;
+  int nmerged = 0;
+  svm_status st;
   // Shared memory of the merged kernel without descriptors (two-stage ring);
   // each query adds its resident descriptor.
   const size_t kMergedSmem = 226 * 1024, kPerQuery = sizeof(MQuery) + 8 + 8 + 4 + 2;
@@ -1415,120 +1468,160 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
     T.nmwords = mp.nmwords;
     return mbatch_smem_bytes(T);
   };
-  if (merged_fixed(2) + kPerQuery > kMergedSmem) mp.place.clear();  // every query takes the per-query kernel
-  std::vector<int> order, legacy;
-  std::vector<MQuery> mqs(nq);
-  std::vector<const int32_t*> gcols;
-  for (int i = 0; i < nq; i++) {
-    BatchQuery& Q = qs[i];
-    struct DimPlace {
-      bool ok = false;
-      MergePlan::Place p;
-    } dp[kMaxDims];
-    bool ok = true;
-    for (int k = 0; k < Q.nsteps && ok; k++) {
-      const Step& st = Q.steps[k];
-      if (st.kind != STEP_PROBE) continue;
-      auto f = mp.place.find({st.col, items[i].plan.dim_tables[st.dim].get()});
-      if (f == mp.place.end() || mp.groups[f->second.group].words == 0) {
-        ok = false;
-        break;
-      }
-      dp[st.dim].ok = true;
-      dp[st.dim].p = f->second;
-    }
-    if (!ok) {
-      legacy.push_back(i);
-      continue;
-    }
-    order.push_back(i);
-    // The merged kernel's descriptor: probe steps become table-slot bit tests
-    // (a folded key range becomes a range step), then the range steps.
-    MQuery M{};
-    M.row_begin = Q.row_begin;
-    M.row_end = Q.row_end;
-    M.ngroups = (uint32_t)Q.ngroups;
-    bool fits = true;
-    for (int k = 0; k < Q.nsteps; k++) {
-      const Step& st = Q.steps[k];
-      if (st.kind == STEP_PROBE) {
-        const MergePlan::Place& pl = dp[st.dim].p;
-        M.probe_tab[M.nprobe++] = (uint8_t)pl.slot;
-        M.gmask |= 1u << pl.group;
-        if (st.lo == INT_MIN && st.hi == INT_MAX) continue;
-      }
-      if (M.nrange == kMaxMRanges) {
-        fits = false;
-        break;
-      }
-      M.range_col[M.nrange] = (uint8_t)st.col;
-      M.range_lo[M.nrange] = st.lo;
-      M.range_hi[M.nrange] = st.hi;
-      M.nrange++;
-    }
-    auto mxt = [&](const Extract& e) {
-      MExtract r{};
-      r.mask = e.mask;
-      r.base = e.base;
-      if (e.dim < 0) {
-        r.src = -1;
-        r.slot = (uint8_t)e.slot;
-        return r;
-      }
-      // A payload field at bit `shift` of the entry sits at pay_bit + shift - 1
-      // of the payload word (the present bit is not carried there).
-      const MergePlan::Place& pl = dp[e.dim].p;
-      r.src = (int8_t)mp.groups[pl.group].word_off;
-      r.slot = (uint8_t)pl.pay_word;
-      r.sg = (uint8_t)mp.groups[pl.group].words;
-      r.shift = (uint8_t)(pl.pay_bit + (e.mask ? e.shift - 1 : 0));
-      if (e.col) {
-        size_t gi = std::find(gcols.begin(), gcols.end(), e.col) - gcols.begin();
-        if (gi == gcols.size()) {
-          if (gcols.size() == (size_t)kMaxGatherCols) {
-            fits = false;
-            return r;
-          }
-          gcols.push_back(e.col);
+  for (;;) {
+    mp = MergePlan{};
+    order.clear();
+    gcols.clear();
+    mqs.assign(nq, MQuery{});
+    plan_merge(x, qs, items, &mp);
+    if (merged_fixed(2) + kPerQuery > kMergedSmem) mp.place.clear();  // every query takes the per-query kernel
+    std::vector<int> legacy;
+    for (int i = 0; i < nq; i++) {
+      BatchQuery& Q = qs[i];
+      struct DimPlace {
+        bool ok = false;
+        MergePlan::Place p;
+      } dp[kMaxDims];
+      bool ok = true;
+      for (int k = 0; k < Q.nsteps && ok; k++) {
+        const Step& st = Q.steps[k];
+        if (st.kind != STEP_PROBE) continue;
+        auto f = mp.place.find({st.col, items[i].plan.dim_tables[st.dim].get()});
+        if (f == mp.place.end() || mp.groups[f->second.group].words == 0) {
+          ok = false;
+          break;
         }
-        r.sg |= (uint8_t)((gi + 1) << 4);
+        dp[st.dim].ok = true;
+        dp[st.dim].p = f->second;
       }
-      M.gmask |= 1u << pl.group;
+      if (!ok) {
+        legacy.push_back(i);
+        continue;
+      }
+      order.push_back(i);
+      // The merged kernel's descriptor: probe steps become table-slot bit tests
+      // (a folded key range becomes a range step), then the range steps.
+      MQuery M{};
+      M.row_begin = Q.row_begin;
+      M.row_end = Q.row_end;
+      M.ngroups = (uint32_t)Q.ngroups;
+      bool fits = true;
+      for (int k = 0; k < Q.nsteps; k++) {
+        const Step& st = Q.steps[k];
+        if (st.kind == STEP_PROBE) {
+          const MergePlan::Place& pl = dp[st.dim].p;
+          M.probe_tab[M.nprobe++] = (uint8_t)pl.slot;
+          M.gmask |= 1u << pl.group;
+          if (st.lo == INT_MIN && st.hi == INT_MAX) continue;
+        }
+        if (M.nrange == kMaxMRanges) {
+          fits = false;
+          break;
+        }
+        M.range_col[M.nrange] = (uint8_t)st.col;
+        M.range_lo[M.nrange] = st.lo;
+        M.range_hi[M.nrange] = st.hi;
+        M.nrange++;
+      }
+      auto mxt = [&](const Extract& e) {
+        MExtract r{};
+        r.mask = e.mask;
+        r.base = e.base;
+        if (e.dim < 0) {
+          r.src = -1;
+          r.slot = (uint8_t)e.slot;
+          return r;
+        }
+        // A payload field at bit `shift` of the entry sits at pay_bit + shift - 1
+        // of the payload word (the present bit is not carried there).
+        const MergePlan::Place& pl = dp[e.dim].p;
+        r.src = (int8_t)mp.groups[pl.group].word_off;
+        r.slot = (uint8_t)pl.pay_word;
+        r.sg = (uint8_t)mp.groups[pl.group].words;
+        r.shift = (uint8_t)(pl.pay_bit + (e.mask ? e.shift - 1 : 0));
+        if (pl.shared && e.mask) {  // the group's shared field holds value - sh.base
+          const MergePlan::Share& sh = mp.share[pl.group];
+          const DimDesc& d = items[i].plan.dim_tables[e.dim]->desc;
+          r.shift = (uint8_t)sh.bit;
+          r.mask = sh.bits >= 32 ? 0xFFFFFFFFu : (1u << sh.bits) - 1u;
+          r.base = (int32_t)((uint32_t)e.base - (uint32_t)d.pay[0].min + (uint32_t)sh.base);
+        }
+        if (e.col) {
+          size_t gi = std::find(gcols.begin(), gcols.end(), e.col) - gcols.begin();
+          if (gi == gcols.size()) {
+            if (gcols.size() == (size_t)kMaxGatherCols) {
+              fits = false;
+              return r;
+            }
+            gcols.push_back(e.col);
+          }
+          r.sg |= (uint8_t)((gi + 1) << 4);
+        }
+        M.gmask |= 1u << pl.group;
+        return r;
+      };
+      M.nkeys = (uint8_t)Q.nkeys;
+      for (int k = 0; k < Q.nkeys; k++) {
+        M.kx[k] = mxt(Q.kx[k]);
+        M.krange[k] = Q.krange[k];
+        M.kstride[k] = Q.kstride[k];
+      }
+      M.nmetrics = (uint8_t)Q.nmetrics;
+      for (int m = 0; m < Q.nmetrics; m++) {
+        M.mform[m] = (uint8_t)Q.mform[m];
+        M.xa[m] = mxt(Q.xa[m]);
+        if (Q.mform[m] != MF_OPND) M.xb[m] = mxt(Q.xb[m]);
+      }
+      if (!fits) {  // more range steps or gather columns than the descriptor holds
+        order.pop_back();
+        legacy.push_back(i);
+        continue;
+      }
+      mqs[i] = M;
+    }
+    nmerged = (int)order.size();
+    // Consumer warps claim a tile's queries in descriptor order and wait for
+    // the last at the tile's end: the most aggregation work first (longest
+    // processing time first) keeps that tail short.
+    std::stable_sort(order.begin(), order.end(), [&](int a, int z) {
+      const StarPlan& pa = items[a].plan;
+      const StarPlan& pz = items[z].plan;
+      return pa.est_pass * (pa.nkeys + pa.nmet + 1) > pz.est_pass * (pz.nkeys + pz.nmet + 1);
+    });
+    order.insert(order.end(), legacy.begin(), legacy.end());
+    if (!nmerged) break;
+    // Build the merged tables; a shared field that two of its tables
+    // disagree on sends those tables to fields of their own, and the batch
+    // is planned again (each round refuses at least one more table).
+    DevBufPtr conflict;
+    if ((st = x->alloc(4 * mp.groups.size(), &conflict, true))) return st;
+    std::vector<std::string> checked(mp.groups.size());
+    auto unchecked = [&](svm_status r) {  // no table leaves unchecked in the cache
+      for (const std::string& k : checked)
+        if (!k.empty()) x->merged_cache.erase(k);
       return r;
     };
-    M.nkeys = (uint8_t)Q.nkeys;
-    for (int k = 0; k < Q.nkeys; k++) {
-      M.kx[k] = mxt(Q.kx[k]);
-      M.krange[k] = Q.krange[k];
-      M.kstride[k] = Q.kstride[k];
+    bool any_checked = false;
+    for (size_t g = 0; g < mp.groups.size(); g++) {
+      if (!mp.groups[g].words) continue;
+      if ((st = merged_table(x, &mp, (int)g, (unsigned int*)conflict->p + g, &checked[g]))) return unchecked(st);
+      any_checked |= !checked[g].empty();
     }
-    M.nmetrics = (uint8_t)Q.nmetrics;
-    for (int m = 0; m < Q.nmetrics; m++) {
-      M.mform[m] = (uint8_t)Q.mform[m];
-      M.xa[m] = mxt(Q.xa[m]);
-      if (Q.mform[m] != MF_OPND) M.xb[m] = mxt(Q.xb[m]);
+    if (!any_checked) break;
+    std::vector<unsigned int> bad(mp.groups.size());
+    cudaError_t ce = cudaMemcpyAsync(bad.data(), conflict->p, 4 * bad.size(), cudaMemcpyDeviceToHost, x->stream);
+    if (!ce) ce = cudaStreamSynchronize(x->stream);
+    if (ce) return unchecked(x->cuda_fail(ce, "merged table check"));
+    bool refused = false;
+    for (size_t g = 0; g < mp.groups.size(); g++) {
+      if (!bad[g]) continue;
+      for (size_t i = 0; i < mp.members[g].size(); i++)
+        if (bad[g] >> i & 1u) x->no_share[mp.members[g][i].first.get()] = mp.members[g][i].first;
+      x->merged_cache.erase(checked[g]);
+      refused = true;
     }
-    if (!fits) {  // more range steps or gather columns than the descriptor holds
-      order.pop_back();
-      legacy.push_back(i);
-      continue;
-    }
-    mqs[i] = M;
+    if (!refused) break;
   }
-  const int nmerged = (int)order.size();
-  // Consumer warps claim a tile's queries in descriptor order and wait for
-  // the last at the tile's end: the most aggregation work first (longest
-  // processing time first) keeps that tail short.
-  std::stable_sort(order.begin(), order.end(), [&](int a, int z) {
-    const StarPlan& pa = items[a].plan;
-    const StarPlan& pz = items[z].plan;
-    return pa.est_pass * (pa.nkeys + pa.nmet + 1) > pz.est_pass * (pz.nkeys + pz.nmet + 1);
-  });
-  order.insert(order.end(), legacy.begin(), legacy.end());
-  svm_status st;
-  if (nmerged)
-    for (size_t g = 0; g < mp.groups.size(); g++)
-      if (mp.groups[g].words && (st = merged_table(x, &mp, (int)g))) return st;
 
   // ---- slots and group numbering in launch order
   std::vector<BatchQuery> dqs(nq);

@@ -204,6 +204,8 @@ struct MergeSrc {           // one dense table placed into a merged table
   int present_bit;          // in word 0
   int pay_word, pay_bit;    // the entry's payload (entry >> 1) ...
   int pay_bits;             // ... of this many bits (0: none)
+  int shared;               // 1: the payload goes to the group's shared field as payload + val_off
+  int32_t val_off;
 };
 
 constexpr int kMaxMergeSrcs = 32;
@@ -212,6 +214,7 @@ struct MergeBuild {
   uint32_t span;
   int words;
   int nsrc;
+  unsigned int* conflict;   // bit i: source i disagreed with the shared field at a key
   MergeSrc src[kMaxMergeSrcs];
 };
 
