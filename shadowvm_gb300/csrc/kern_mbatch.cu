@@ -50,6 +50,7 @@ __device__ __forceinline__ int row_slot(int r) { return ((r & 31) << 5) | ((r >>
 constexpr int kBmStride = kChunks + 1;      // a table's bitmap row, padded (conflict-free stores)
 static_assert(sizeof(MQuery) == 240 && sizeof(MExtract) == 12, "descriptor layout");
 constexpr int kDenseRows = 256;             // live rows above which a range test runs on every row
+constexpr int kAggRing = 64;                // surviving-row ring per consumer warp (uint16 rows)
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
@@ -146,7 +147,8 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
 // L + 32 i (i = 0..31) as bit i of one mask word, so every per-row shared
 // memory read of a lane hits its own bank.
 __device__ __forceinline__ void mquery_tile(const MQuery& Q, const BatchParams& B, const int32_t* stage,
-                                            const uint32_t* mw, const uint32_t* bm, int lo, int hi, int lane) {
+                                            const uint32_t* mw, const uint32_t* bm, int lo, int hi, int lane,
+                                            uint32_t lt, uint16_t* ring) {
   // bits i with lo <= L + 32 i < hi
   const int ia = lo > lane ? (lo - lane + 31) >> 5 : 0;
   const int ib = hi > lane ? ((hi - 1 - lane) >> 5) + 1 : 0;  // exclusive
@@ -189,8 +191,7 @@ __device__ __forceinline__ void mquery_tile(const MQuery& Q, const BatchParams& 
   const MExtract* xb = Q.xb;
   const uint8_t* mf = Q.mform;
   long long acc[kMaxMetrics] = {0, 0, 0};
-  for (uint32_t bb = m; bb; bb &= bb - 1) {
-    const int row = 32 * (__ffs(bb) - 1) + lane;
+  auto aggregate = [&](int row) {
     uint32_t gi = 0;
     bool in_range = true;
 #pragma unroll
@@ -203,7 +204,7 @@ __device__ __forceinline__ void mquery_tile(const MQuery& Q, const BatchParams& 
     }
     if (!in_range) {
       raise_error(B.error, DERR_KEY_RANGE);
-      continue;
+      return;
     }
 #pragma unroll
     for (int mi = 0; mi < kMaxMetrics; mi++) {
@@ -222,6 +223,29 @@ __device__ __forceinline__ void mquery_tile(const MQuery& Q, const BatchParams& 
       }
     }
     if (nkeys) sums[(size_t)nm * G + gi] = 1ull;  // the group has a row
+  };
+  // The warp's surviving rows, balanced over its lanes: a lane walking only
+  // its own rows would hold the warp for as many steps as its busiest lane.
+  // Each step appends every lane's next row (one per lane, consecutive
+  // entries from distinct lanes) to the warp's 64-entry ring; every 32
+  // entries, and once at the end, the lanes take one entry each.
+  uint32_t bb = m, wp = 0, rp = 0;  // ring write / read positions (warp-uniform)
+  for (;;) {
+    const uint32_t has = __ballot_sync(0xffffffffu, bb != 0u);
+    if (bb) {
+      const int j = __ffs(bb) - 1;
+      bb &= bb - 1;
+      ring[(wp + __popc(has & lt)) & (kAggRing - 1)] = (uint16_t)(32 * j + lane);
+    }
+    wp += __popc(has);
+    if (wp - rp >= 32u || (has == 0u && wp != rp)) {
+      __syncwarp();
+      const uint32_t n = wp - rp < 32u ? wp - rp : 32u;
+      if ((uint32_t)lane < n) aggregate(ring[(rp + lane) & (kAggRing - 1)]);
+      rp += n;
+      __syncwarp();  // read before the next steps overwrite the slots
+    }
+    if (has == 0u) break;
   }
   if (nkeys == 0) {
 #pragma unroll
@@ -275,6 +299,7 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
   long long* qhi = qlo + nq;
   uint32_t* qg = reinterpret_cast<uint32_t*>(qhi + nq);
   uint16_t* act = reinterpret_cast<uint16_t*>(qg + nq);
+  uint16_t* aggring = act + nq;  // kAggRing per consumer warp
   if (tid == 0) {
     for (int s = 0; s < nst; s++) {
       mbar_init(&full[s], 1);
@@ -437,7 +462,7 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
       const int q = act[k];
       const long long lo = qlo[q] > tile_start ? qlo[q] - tile_start : 0;
       const long long hi = qhi[q] < tile_end ? qhi[q] - tile_start : kTileRows;
-      mquery_tile(sq[q], B, stage, mw, bm, (int)lo, (int)hi, lane);
+      mquery_tile(sq[q], B, stage, mw, bm, (int)lo, (int)hi, lane, lt, aggring + warp * kAggRing);
     }
     consumer_bar();
     if (tid == 0) {
@@ -495,7 +520,8 @@ cudaError_t launch_merge_build(const MergeBuild& m, uint32_t* out, cudaStream_t 
 
 size_t mbatch_smem_bytes(const BatchParams& b) {
   return (size_t)b.nstages * b.ncols * kTileRows * 4 + 2 * (size_t)b.nmwords * kSlots * 4 +
-         (size_t)kMaxMergedTables * kBmStride * 4 + (size_t)b.nqueries * (sizeof(MQuery) + 8 + 8 + 4 + 2) + 16;
+         (size_t)kMaxMergedTables * kBmStride * 4 + (size_t)b.nqueries * (sizeof(MQuery) + 8 + 8 + 4 + 2) +
+         (size_t)kMBatchWarps * kAggRing * 2 + 16;
 }
 
 int mbatch_grid_size(const BatchParams& b, size_t smem) {
