@@ -1124,8 +1124,11 @@ svm_status resolve_strings(Ctx* x, Bound* b, const ObjectPtr& src, const std::ve
 }
 
 // Binds a pipeline and resolves its pre_pipeline_id objects.
-svm_status resolve(Ctx* x, const svm_pipeline* p, Bound* b, ObjectPtr* src, std::vector<ObjectPtr>* refs) {
-  svm_status st = bind(x, p, b);
+// Binds `p` (unless `bound`: *b already holds its binding) and finds its
+// source and joined objects.
+svm_status resolve(Ctx* x, const svm_pipeline* p, Bound* b, ObjectPtr* src, std::vector<ObjectPtr>* refs,
+                   bool bound = false) {
+  svm_status st = bound ? SVM_OK : bind(x, p, b);
   if (st) return st;
   if (p->npre < 1 || !p->pre_pipeline_id || !p->pre_pipeline_id[0])
     return x->fail(SVM_E_INVALID_ARG, "pipeline " + b->id + " has no source object (pre_pipeline_id[0])");
@@ -1154,10 +1157,10 @@ struct BatchItem {
 // Cost model of a fold, in picoseconds, measured on GB300 with the 256-query
 // star-schema mix over a 600 M-row table: one query alone costs about 5.4 ps
 // per row it reads plus ~30 us of launch, finalize and result handling; the
-// batched launch costs about 50 ps per row of the union of the queries'
+// batched launch costs about 46 ps per row of the union of the queries'
 // ranges (the shared scan, merged-table lookups, bitmaps and per-tile
-// bookkeeping: 30.1 ms for the 600 M-row union with the query work removed)
-// plus 0.39 ps per query row (9.9 ms for the mix's 25.5 G query-rows), plus
+// bookkeeping: 27.6 ms for the 600 M-row union with the query work removed)
+// plus 0.25 ps per query row (6.4 ms for the mix's 25.5 G query-rows), plus
 // ~100 us.  The cheaper way runs.
 bool batch_is_cheaper(const std::vector<BatchItem>& items) {
   std::vector<std::pair<long long, long long>> iv;
@@ -1181,7 +1184,7 @@ bool batch_is_cheaper(const std::vector<BatchItem>& items) {
     }
   }
   if (ce > cb) uni += (double)(ce - cb);
-  const double batch = 50.0 * uni + 0.39 * rows + 100e6;
+  const double batch = 46.0 * uni + 0.25 * rows + 100e6;
   return batch < single;
 }
 
@@ -1807,13 +1810,13 @@ svm_status run_batch(Ctx* x, int n, const svm_pipeline* p) {
   // reduce pipelines over the same fact table share one batched launch.  A
   // batch in which some pipeline reads a reduce pipeline's output runs in order.
   std::vector<char> reduce(n);
+  std::vector<Bound> bounds(n);
   std::set<std::string> reduce_ids;
   for (int i = 0; i < n; i++) {
-    Bound b;
-    svm_status st = bind(x, &p[i], &b);
+    svm_status st = bind(x, &p[i], &bounds[i]);
     if (st) return st;
-    reduce[i] = b.is_reduce;
-    if (b.is_reduce) reduce_ids.insert(b.id);
+    reduce[i] = bounds[i].is_reduce;
+    if (bounds[i].is_reduce) reduce_ids.insert(bounds[i].id);
   }
   for (int i = 0; i < n; i++)
     for (int j = 0; j < p[i].npre; j++)
@@ -1830,12 +1833,12 @@ svm_status run_batch(Ctx* x, int n, const svm_pipeline* p) {
   }
   std::map<const void*, std::vector<BatchItem>> groups;
   for (int i = 0; i < n; i++) {
-    Bound b;
+    if (!reduce[i]) continue;
+    Bound& b = bounds[i];  // bound above (binding parses the pipeline alone, reading no object)
     ObjectPtr src;
     std::vector<ObjectPtr> refs;
-    svm_status st = resolve(x, &p[i], &b, &src, &refs);
+    svm_status st = resolve(x, &p[i], &b, &src, &refs, true);
     if (st) return st;
-    if (!b.is_reduce) continue;
     BatchItem it;
     it.id = b.id;
     it.src = src;
