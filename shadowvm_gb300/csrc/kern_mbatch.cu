@@ -288,6 +288,8 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
   __shared__ long long s_tile;
   __shared__ int s_next, s_na;
   __shared__ uint32_t s_need;
+  __shared__ int s_list_na[2];          // per lookup buffer: the fill's list of the tile's queries
+  __shared__ uint32_t s_list_need[2];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ncols = B.ncols, nst = B.nstages, nq = B.nqueries;
   const size_t mw_words = (size_t)B.nmwords * kSlots;
@@ -298,15 +300,15 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
   long long* qlo = reinterpret_cast<long long*>(sq + nq);
   long long* qhi = qlo + nq;
   uint32_t* qg = reinterpret_cast<uint32_t*>(qhi + nq);
-  uint16_t* act = reinterpret_cast<uint16_t*>(qg + nq);
-  uint16_t* aggring = act + nq;  // kAggRing per consumer warp
+  uint16_t* act = reinterpret_cast<uint16_t*>(qg + nq);  // two lists of nq, one per lookup buffer
+  uint16_t* aggring = act + 2 * nq;                       // kAggRing per consumer warp
   if (tid == 0) {
     for (int s = 0; s < nst; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; b++) {
-      mbar_init(&fill_full[b], 32 * kFillWarps);  // one arrival per fill lane
+      mbar_init(&fill_full[b], 32 * kFillWarps + 1);  // each fill lane's gathers + the list
       mbar_init(&fill_empty[b], 1);
     }
     mbar_fence_init();
@@ -365,11 +367,23 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
       last_seen = i;
       const long long t = stage_tile[s];
       if (t < 0) {
+        if (tma && lane == 0) mbar_arrive(&fill_full[b]);  // the list's arrival
         mbar_arrive(&fill_full[b]);  // every fill lane: lets the consumers reach the end marker
         break;
       }
+      // Fill warp 0 lists the tile's queries for the consumers (one tile
+      // ahead of them), so no consumer warp holds the others while it lists.
       int na;
-      const uint32_t need = tile_queries(qlo, qhi, qg, nq, a0 + t * kTileRows, nullptr, false, lane, lt, &na);
+      const uint32_t need =
+          tile_queries(qlo, qhi, qg, nq, a0 + t * kTileRows, act + (size_t)b * nq, tma, lane, lt, &na);
+      if (tma) {
+        if (lane == 0) {
+          s_list_na[b] = na;
+          s_list_need[b] = need;
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&fill_full[b]);  // the list
+      }
       const int32_t* stage = ring + (size_t)s * ncols * kTileRows;
       uint32_t* mwb = mwbuf + (size_t)b * mw_words;
       // The next tile's copies.  With three or more stages its slot held
@@ -403,24 +417,15 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
   for (long long i = 0;; i++) {
     const int s = (int)(i % nst), b = (int)(i & 1);
     const uint32_t sp = (uint32_t)((i / nst) & 1), bp = (uint32_t)((i / 2) & 1);
-    // Warp 0 waits for the tile, lists its queries and the probe groups they
-    // need; the other warps take the list from shared memory.
-    if (warp == 0) {
-      long long t0 = -2;
-      if (lane == 0) {
-        const bool good = mbar_wait_bounded(&fill_full[b], bp, kPolls) && mbar_wait_bounded(&full[s], sp, kPolls);
-        t0 = good ? stage_tile[s] : -2;
-        s_next = 0;
-      }
-      t0 = __shfl_sync(0xffffffffu, t0, 0);
-      int na0 = 0;
-      uint32_t need0 = 0;
-      if (t0 >= 0) need0 = tile_queries(qlo, qhi, qg, nq, a0 + t0 * kTileRows, act, true, lane, lt, &na0);
-      if (lane == 0) {
-        s_tile = t0;
-        s_na = na0;
-        s_need = need0;
-      }
+    // Warp 0 waits for the tile and hands its query list (written by the
+    // fill warps) to the other warps.
+    if (warp == 0 && lane == 0) {
+      const bool good = mbar_wait_bounded(&fill_full[b], bp, kPolls) && mbar_wait_bounded(&full[s], sp, kPolls);
+      const long long t0 = good ? stage_tile[s] : -2;
+      s_next = 0;
+      s_tile = t0;
+      s_na = t0 >= 0 ? s_list_na[b] : 0;
+      s_need = t0 >= 0 ? s_list_need[b] : 0u;
     }
     consumer_bar();
     const long long t = s_tile;
@@ -459,7 +464,7 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
       if (lane == 0) k = atomicAdd(&s_next, 1);
       k = __shfl_sync(0xffffffffu, k, 0);
       if (k >= na) break;
-      const int q = act[k];
+      const int q = act[(size_t)b * nq + k];
       const long long lo = qlo[q] > tile_start ? qlo[q] - tile_start : 0;
       const long long hi = qhi[q] < tile_end ? qhi[q] - tile_start : kTileRows;
       mquery_tile(sq[q], B, stage, mw, bm, (int)lo, (int)hi, lane, lt, aggring + warp * kAggRing);
@@ -520,7 +525,7 @@ cudaError_t launch_merge_build(const MergeBuild& m, uint32_t* out, cudaStream_t 
 
 size_t mbatch_smem_bytes(const BatchParams& b) {
   return (size_t)b.nstages * b.ncols * kTileRows * 4 + 2 * (size_t)b.nmwords * kSlots * 4 +
-         (size_t)kMaxMergedTables * kBmStride * 4 + (size_t)b.nqueries * (sizeof(MQuery) + 8 + 8 + 4 + 2) +
+         (size_t)kMaxMergedTables * kBmStride * 4 + (size_t)b.nqueries * (sizeof(MQuery) + 8 + 8 + 4 + 4) +
          (size_t)kMBatchWarps * kAggRing * 2 + 16;
 }
 

@@ -1463,7 +1463,7 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
   svm_status st;
   // Shared memory of the merged kernel without descriptors (two-stage ring);
   // each query adds its resident descriptor.
-  const size_t kMergedSmem = 226 * 1024, kPerQuery = sizeof(MQuery) + 8 + 8 + 4 + 2;
+  const size_t kMergedSmem = 226 * 1024, kPerQuery = sizeof(MQuery) + 8 + 8 + 4 + 4;
   auto merged_fixed = [&](int nst) {
     BatchParams T{};
     T.ncols = (int)ucols.size();
