@@ -53,7 +53,8 @@ def measured_hbm_peak():
 
 
 def committed_traffic(config: int):
-    """DRAM bytes per fact row of the star kernel from the committed ncu summary."""
+    """DRAM traffic of the workload's kernel from the committed ncu summaries: per
+    fact row for the star kernel, per shared-scan byte for the batch kernel."""
     p = os.path.join(ROOT, "profiles", "star_kernel_traffic.json")
     try:
         d = json.load(open(p))
@@ -420,8 +421,11 @@ def batched_arm(args):
     scan_bytes = 4 * len(ucols) * urows
     k_s = m["device_ms"]["batch_kernel"] / 1e3
     peak, peak_src = measured_hbm_peak()
+    tr = committed_traffic(3)
     roofline = {"bound": "hbm", "achieved": scan_bytes / k_s / 1e9, "peak": peak, "unit": "GB/s",
-                "frac": scan_bytes / k_s / 1e9 / peak, "traffic": None, "kernel": "mbatch_kernel",
+                "frac": scan_bytes / k_s / 1e9 / peak,
+                "traffic": tr["dram_bytes_per_scan_byte"] * scan_bytes if tr else None,
+                "traffic_source": tr.get("source") if tr else None, "kernel": "mbatch_kernel",
                 "kernel_ms": k_s * 1e3, "algorithmic_bytes_per_launch": scan_bytes,
                 "unshared_bytes": int(sum(4 * len(used[q.shape]) * q.nrows for q in bw.queries)),
                 "peak_source": peak_src,
