@@ -7,8 +7,8 @@ For every case below it runs the workload through the reference's OWN
 CodeGen and runtime headers (oracle mode "ref", built by oracle/build_ref.sh
 from the reference sources) and records the merged, key-sorted result.  For
 the code generator it records the SHA-256 of the host code the reference's
-CodeGen emits for each pipeline (the text itself is not stored).  The GPU machine
-has no reference tree, so the tests read these files instead.
+CodeGen emits for each pipeline (the text itself is not stored).  A GPU host
+without the reference tree runs the tests against these files instead.
 """
 from __future__ import annotations
 
