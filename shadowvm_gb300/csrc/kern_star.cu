@@ -365,6 +365,12 @@ template <int kAgg, bool kProg>
 __global__ void __launch_bounds__(kStarThreads, 3) star_kernel(const __grid_constant__ StarParams P) {
   extern __shared__ __align__(128) uint8_t dyn[];
   __shared__ StarSmem S;
+  // The filter steps, copied once per block: the step loop reads them with a
+  // runtime index, which from the kernel parameters costs a constant-bank
+  // load per field per warp and tile (3.87 -> 3.57 ms on the 600 M-row
+  // four-dimension star query when read from shared memory instead).
+  __shared__ Step s_steps[kMaxSteps];
+  static_assert(sizeof(Step) % 4 == 0, "steps are copied as 32-bit words");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ncols = P.ncols, nst = P.nstages;
   const size_t ring_bytes = (size_t)nst * ncols * kTileRows * 4;
@@ -380,6 +386,8 @@ __global__ void __launch_bounds__(kStarThreads, 3) star_kernel(const __grid_cons
   uint32_t* aggbuf = reinterpret_cast<uint32_t*>(s_cnt + (kAgg == AGG_DENSE_SMEM ? G : 0));
   const bool deferred = !kProg && P.agg_words > 0;
 
+  for (int i = tid; i < P.nsteps * (int)(sizeof(Step) / 4); i += blockDim.x)
+    reinterpret_cast<uint32_t*>(s_steps)[i] = reinterpret_cast<const uint32_t*>(P.steps)[i];
   if (tid == 0) {
     for (int s = 0; s < nst; s++) {
       mbar_init(&S.full[s], 1);
@@ -451,7 +459,7 @@ __global__ void __launch_bounds__(kStarThreads, 3) star_kernel(const __grid_cons
       // are kept per row in shared memory; the warp stops once no row lives.
       for (int k = 0; k < P.nsteps; k++) {
         if (!__any_sync(0xffffffffu, mask)) break;
-        const Step& st = P.steps[k];
+        const Step& st = s_steps[k];
         const int4 v = reinterpret_cast<const int4*>(wstage + st.col * kTileRows)[lane];
         const int32_t key[4] = {v.x, v.y, v.z, v.w};
         const uint32_t span = (uint32_t)st.hi - (uint32_t)st.lo;
