@@ -399,7 +399,9 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
       };
       if (tma && early) next_tile();
       for (uint32_t mm = need; mm; mm &= mm - 1) {
-        const ProbeGroup& G = B.probe[__ffs(mm) - 1];
+        // A register copy: the gathers' asm clobbers memory, which would
+        // otherwise reload the group's fields for every row.
+        const ProbeGroup G = B.probe[__ffs(mm) - 1];
         for (int row = fw * kFillRows + lane; row < (fw + 1) * kFillRows; row += 32)
           fill_issue(G, stage, mwb, row, pol_tab);
       }
