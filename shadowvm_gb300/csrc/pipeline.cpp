@@ -1155,7 +1155,7 @@ struct BatchItem {
 };
 
 // Cost model of a fold, in picoseconds, measured on GB300 with the 256-query
-// star-schema mix over a 600 M-row table: one query alone costs about 5.4 ps
+// star-schema mix over a 600 M-row table: one query alone costs about 4.6 ps
 // per row it reads plus ~30 us of launch, finalize and result handling; the
 // batched launch costs about 46 ps per row of the union of the queries'
 // ranges (the shared scan, merged-table lookups, bitmaps and per-tile
@@ -1169,7 +1169,7 @@ bool batch_is_cheaper(const std::vector<BatchItem>& items) {
     const long long b = it.plan.P.row_begin, e = it.plan.empty_filter ? b : it.plan.P.row_end;
     iv.push_back({b, e});
     rows += (double)(e - b);
-    single += 5.4 * (double)(e - b) + 30e6;
+    single += 4.6 * (double)(e - b) + 30e6;
   }
   std::sort(iv.begin(), iv.end());
   double uni = 0;
