@@ -1,0 +1,41 @@
+"""bench.py's CPU-side pieces: the roofline traffic it reports comes from the
+committed ncu summaries (per fact row for the star kernel, per shared-scan
+byte for the batch kernel), and its command line parses."""
+import os
+import subprocess
+import sys
+
+import bench
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_star_kernel_traffic_is_committed():
+    tr = bench.committed_traffic(2)
+    assert tr is not None
+    # five int32 columns read once: 20 B per fact row, a little above for the
+    # probe tables and the group slots
+    assert 20.0 <= tr["dram_bytes_per_row"] < 20.5
+    assert "star_kernel_config2.md" in tr["source"]
+    # the String-dimension query runs the same kernel over the same fact columns
+    assert bench.committed_traffic(5) == tr
+
+
+def test_batch_kernel_traffic_is_committed():
+    tr = bench.committed_traffic(3)
+    assert tr is not None
+    # the shared scan reads the union of the queries' columns once
+    assert 1.0 <= tr["dram_bytes_per_scan_byte"] < 1.05
+    assert "mbatch_kernel_config3.md" in tr["source"]
+
+
+def test_unknown_workload_has_no_committed_traffic():
+    assert bench.committed_traffic(4) is None
+
+
+def test_command_line_parses():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--help"], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr
+    for flag in ("--gpus", "--steps", "--warmup", "--impl", "--config"):
+        assert flag in r.stdout
