@@ -10,6 +10,7 @@
 """
 from __future__ import annotations
 
+import re
 from dataclasses import dataclass, field
 
 from .proto import ObjectInfo, OperatorInfo, OpType, PipelineInfo, ValType, create_schema
@@ -97,10 +98,20 @@ def fact_pipeline(pid: str, source: str, src_schema: ObjectInfo, dims: list[str]
 # ------------------------------------------------------------------ Java DSL mirror
 @dataclass
 class Table:
-    """A named object with named columns (ObjectSchema in the Java front end)."""
+    """A named object with named columns (ObjectSchema in the Java front end).
+    A column named None has no name; one named "" is known as `$UNKNOWN`
+    (PipelineBuilder.java:60-66)."""
     id: str
-    columns: list[str]
+    columns: list[str | None]
     schema: ObjectInfo = field(default_factory=ObjectInfo)
+
+
+def _java_split(s: str, regex: str) -> list[str]:
+    """java.lang.String.split(regex): trailing empty pieces dropped."""
+    parts = re.split(regex, s)
+    while len(parts) > 1 and parts[-1] == "":
+        parts.pop()
+    return parts
 
 
 class PipelineBuilder:
@@ -109,6 +120,7 @@ class PipelineBuilder:
     def __init__(self, pid: str, source: Table, output: ObjectInfo):
         self.info = PipelineInfo(id=pid)
         self.output = output
+        self.out_names: list[str | None] = [None] * len(output.column_list)  # set by map()
         self.tables: list[Table] = []
         self.names: dict[str, str] = {}
         self._add_table(source)
@@ -120,11 +132,13 @@ class PipelineBuilder:
         self.tables.append(t)
         self.info.pre_pipeline_id.append(t.id)
         for c, name in enumerate(t.columns):
-            if name:
-                self.names["$" + name] = f"$({k}.{c})"
+            if name is not None:  # a later table's column of the same name wins
+                self.names["$" + name if name else "$UNKNOWN"] = f"$({k}.{c})"
 
     def replace(self, expr: str) -> str:
-        """PipelineBuilder.replaceExpression: longest names first."""
+        """PipelineBuilder.replaceExpression: plain text replacement of every
+        known `$name`, names in descending order (a TreeSet walked backwards),
+        so a name goes before any shorter name that prefixes it."""
         for key in sorted(self.names, reverse=True):
             expr = expr.replace(key, self.names[key])
         return expr
@@ -137,7 +151,18 @@ class PipelineBuilder:
         return self._op(OpType.Filter, {"predication": self.replace(cond)})
 
     def map(self, *cols: str):
-        return self._op(OpType.Map, {"select": ",".join(self.replace(c) for c in cols)})
+        """Also names output column i as the DSL does (PipelineBuilder.java:
+        106-117): the text after the `$`, or, when the rewritten expression
+        splits on the regex "/." (a '/' and the character after it), the
+        second piece."""
+        out = []
+        for i, c in enumerate(cols):
+            new = self.replace(c)
+            parts = _java_split(new[1:], "/.")
+            if i < len(self.out_names):
+                self.out_names[i] = c[1:] if len(parts) == 1 else parts[1]
+            out.append(new)
+        return self._op(OpType.Map, {"select": ",".join(out)})
 
     def join_with(self, table: Table, lkey: str, rkey: str):
         self._add_table(table)
@@ -149,3 +174,8 @@ class PipelineBuilder:
     def sink(self) -> PipelineInfo:
         self._op(OpType.Sink, {})
         return self.info
+
+    def table(self) -> Table:
+        """This pipeline's output as a table another builder can join: its id
+        and the column names map() gave (Pipeline.schema() in the DSL)."""
+        return Table(self.info.id, list(self.out_names), self.output)

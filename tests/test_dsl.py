@@ -1,0 +1,77 @@
+"""The Java DSL mirror (pipeline.PipelineBuilder) against the DSL's own
+known answers and rules (java_vRDD/src/main/java/ShadowVM/PipelineBuilder.java:
+57-147; the test java_vRDD/src/test/java/RDDTest.java:16-31).  The tables are
+the Star Schema Benchmark's lineorder and date in the column order the Java
+test helper declares them (SSBHelper.java:11-55)."""
+import re
+
+from shadowvm_gb300.pipeline import PipelineBuilder, Table
+from shadowvm_gb300.proto import ObjectInfo, OpType, ValType, create_schema
+
+LINEORDER = ["lo_orderkey", "lo_linenumber", "lo_custkey", "lo_partkey", "lo_suppkey", "lo_orderdate",
+             "lo_orderpriority", "lo_shippriority", "lo_quantity", "lo_extendedprice", "lo_ordtotalprice",
+             "lo_discount", "lo_revenue", "lo_supplycost", "lo_tax", "lo_commitdate", "lo_shipmode"]
+DATE = ["d_datekey", "d_date", "d_dayofweek", "d_month", "d_year", "d_yearmonthnum", "d_yearmonth",
+        "d_daynuminweek", "d_daynuminmonth", "d_daynuminyear", "d_monthnuminyear", "d_weeknuminyear",
+        "d_sellingseason", "d_lastdayinweekfl", "d_lastdayinmonthfl", "d_holidayfl", "d_weekdayfl"]
+
+
+def _schema(n):
+    return create_schema([ValType.Int32] * n, [4] * n)
+
+
+def test_replace_expression_known_answers():
+    """RDDTest.TestReplaceExpr: lineorder joined with date."""
+    pb = PipelineBuilder("testReplace", Table("lineorder", LINEORDER), ObjectInfo())
+    pb.join_with(Table("date", DATE), "", "")
+    assert pb.replace("$d_year==1997 || $d_year==1998") == "$(1.4)==1997 || $(1.4)==1998"
+    assert pb.replace("($lo_revenue-$lo_supplycost)/100") == "($(0.12)-$(0.13))/100"
+
+
+def test_longer_names_are_replaced_before_their_prefixes():
+    pb = PipelineBuilder("p", Table("date", DATE), ObjectInfo())
+    assert pb.replace("$d_yearmonthnum + $d_yearmonth + $d_year") == "$(0.5) + $(0.6) + $(0.4)"
+    # plain text replacement: an unknown name is left as it is
+    assert pb.replace("$d_century > 1") == "$d_century > 1"
+
+
+def test_map_names_its_outputs_and_joins_use_them():
+    """map() names output column i after its expression; a pipeline joined
+    later is addressed through those names."""
+    dim = PipelineBuilder("q-date", Table("date", DATE), _schema(2))
+    dim.filter("$d_year == 1993").map("$d_datekey", "$d_year")
+    dim_info = dim.sink()
+    assert dim.table().columns == ["d_datekey", "d_year"]
+    assert dim_info.workflow[-2].args == {"select": "$(0.0),$(0.4)"}
+    fact = PipelineBuilder("q", Table("lineorder", LINEORDER), _schema(2))
+    fact.filter("$lo_discount >= 1 && $lo_discount <= 3 && $lo_quantity < 25")
+    fact.join_with(dim.table(), "$lo_orderdate", "$d_datekey")
+    fact.reduce_by("$d_year", "($lo_extendedprice*$lo_discount)/1000")
+    info = fact.sink()
+    assert info.pre_pipeline_id == ["lineorder", "q-date"]
+    ops = {op.type: op.args for op in info.workflow}
+    assert ops[OpType.Filter] == {"predication": "$(0.11) >= 1 && $(0.11) <= 3 && $(0.8) < 25"}
+    assert ops[OpType.JoinWith] == {"lkey": "$(0.5)", "rkey": "$(1.0)"}
+    assert ops[OpType.ReduceBy] == {"dim": "$(1.1)", "metric": "($(0.9)*$(0.11))/1000"}
+    # every name was rewritten (the check the DSL's own SSB tests make)
+    for op in info.workflow:
+        for v in op.args.values():
+            assert not re.search(r"\$(?!\()", v), v
+
+
+def test_map_output_names_follow_the_dsl_split():
+    """The name is the text after '$' unless the rewritten expression splits
+    on the regex "/." ('/' and the next character), then the second piece;
+    trailing empty pieces do not count, as in java.lang.String.split."""
+    pb = PipelineBuilder("m", Table("lineorder", LINEORDER), _schema(3))
+    pb.map("$lo_revenue/100", "$lo_revenue/1", "$lo_tax")
+    assert pb.table().columns == ["00", "lo_revenue/1", "lo_tax"]
+
+
+def test_unnamed_and_repeated_columns():
+    """An empty column name is known as $UNKNOWN, a missing one not at all;
+    of two tables with the same column name the later one wins."""
+    pb = PipelineBuilder("u", Table("a", ["k", "", None, "v"]), ObjectInfo())
+    assert pb.replace("$UNKNOWN + $k") == "$(0.1) + $(0.0)"
+    pb.join_with(Table("b", ["v", "w"]), "$k", "$v")
+    assert pb.replace("$v") == "$(1.0)"
