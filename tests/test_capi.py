@@ -37,3 +37,26 @@ def test_host_only_calls(built_lib):
     assert cfg.hash_char_signed == 1
     assert lib.svm_last_error(None) == b"null context"
     assert lib.svm_run_pipeline(None, None) == capi.E_INVALID_ARG
+
+
+def test_headers_are_plain_c(tmp_path):
+    """The boundary is a C ABI: every header compiles as strict C99 on its
+    own (what a cgo, JNI or N-API stub includes), and a C program can take
+    the address of every declared entry point."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        names = sorted(declared(h))
+        src = tmp_path / "use.c"
+        src.write_text(f'#include "{h}"\n' + "void *entry_points[] = {\n" +
+                       "".join(f"  (void *)&{n},\n" for n in names) + "};\n")
+        r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-Wno-pedantic",
+                            "-fsyntax-only", str(src)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only", "-x", "c",
+                            h], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
