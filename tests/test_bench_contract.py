@@ -39,3 +39,23 @@ def test_command_line_parses():
     assert r.returncode == 0, r.stderr
     for flag in ("--gpus", "--steps", "--warmup", "--impl", "--config"):
         assert flag in r.stdout
+
+
+def test_reference_arm_prints_its_contract_line():
+    """--impl reference times the reference's generated CPU path (the oracle
+    port) on a bounded sample and prints one JSON line with the keys the
+    comparison reads; here on a tiny config-0 sample."""
+    import json
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--config", "0",
+                        "--cpu-sample-rows", "200000", "--steps", "1", "--warmup", "3"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == "fact rows/s" and d["unit"] == "rows/s"
+    assert d["value"] > 0 and d["higher_is_better"] is True
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"].startswith("config 0")
