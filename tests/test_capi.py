@@ -60,3 +60,58 @@ def test_headers_are_plain_c(tmp_path):
         r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only", "-x", "c",
                             h], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def _status_functions():
+    """(name, parameter list) of every header function returning svm_status."""
+    out = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for name, params in re.findall(r"\bsvm_status\s+(svm_[a-z0-9_]+)\s*\(([^)]*)\)", text):
+            out.append((name, [p.strip() for p in params.split(",") if p.strip()]))
+    return out
+
+
+def test_every_entry_point_rejects_a_null_context(built_lib):
+    """Each call that takes a context answers SVM_E_INVALID_ARG to a null one
+    (and null / zero arguments) before it touches the GPU."""
+    lib = ctypes.CDLL(built_lib)
+    checked = 0
+    for name, params in _status_functions():
+        if not params or not re.match(r"(const\s+)?svm_ctx\s*\*", params[0]):
+            continue
+        args = []
+        for p in params:
+            if "*" in p:
+                args.append(ctypes.c_void_p(None))
+            elif "unsigned long long" in p or "uint64_t" in p or "size_t" in p:
+                args.append(ctypes.c_ulonglong(0))
+            else:
+                args.append(ctypes.c_int(0))
+        fn = getattr(lib, name)
+        fn.restype = ctypes.c_int
+        assert fn(*args) == capi.E_INVALID_ARG, name
+        checked += 1
+    assert checked >= 19
+
+
+def test_init_validates_before_the_gpu(built_lib):
+    lib = capi.load(built_lib)
+    cfg = capi.svm_config()
+    lib.svm_config_default(ctypes.byref(cfg))
+    ctx = ctypes.c_void_p()
+    assert lib.svm_init(ctypes.byref(cfg), None) == capi.E_INVALID_ARG
+    bad = capi.svm_config()
+    lib.svm_config_default(ctypes.byref(bad))
+    bad.tuple_per_bulk = 0
+    assert lib.svm_init(ctypes.byref(bad), ctypes.byref(ctx)) == capi.E_INVALID_ARG and not ctx.value
+    lib.svm_config_default(ctypes.byref(bad))
+    bad.join_mode = 7
+    assert lib.svm_init(ctypes.byref(bad), ctypes.byref(ctx)) == capi.E_INVALID_ARG and not ctx.value
+    # a valid configuration: a context where a GPU is present, else a CUDA error and no context
+    st = lib.svm_init(ctypes.byref(cfg), ctypes.byref(ctx))
+    if st == capi.OK:
+        lib.svm_destroy(ctx)
+    else:
+        assert st == capi.E_CUDA and not ctx.value
