@@ -113,7 +113,7 @@ class Lexer {
       return true;
     }
     // A string literal, its quotes optionally backslash-escaped as the Java
-    // DSL writes them (StrCmp($p_category,\"MFGR#12\",8)); C escapes \\ \" \0.
+    // DSL writes them (StrCmp($(1.2),\"abc\",3)); C escapes \\ \" \0.
     if (c == '"' || (c == '\\' && i_ + 1 < s_.size() && s_[i_ + 1] == '"')) {
       const bool escaped = c == '\\';
       size_t j = i_ + (escaped ? 2 : 1);
