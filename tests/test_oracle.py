@@ -42,6 +42,20 @@ def test_port_reproduces_reference_results(name):
     np.testing.assert_array_equal(sums, gs)
 
 
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference-compiled checker not built (oracle/_ref)")
+@pytest.mark.parametrize("name", sorted(GOLDEN))
+def test_fixtures_equal_the_live_reference(name):
+    """Where the reference tree is present, its own CodeGen and runtime headers
+    (oracle mode "ref") reproduce every committed fixture now, not only when
+    the fixtures were written."""
+    case = GOLDEN[name]
+    w = build_case(case)
+    (keys, sums), _ = oracle.run_workload(w, "ref", threads=4)
+    gk, gs = golden_arrays(case, w.key_num)
+    np.testing.assert_array_equal(keys, gk)
+    np.testing.assert_array_equal(sums, gs)
+
+
 @pytest.mark.parametrize("name", sorted(GOLDEN))
 def test_exact_evaluator_agrees_where_reference_drops_nothing(name):
     case = GOLDEN[name]
