@@ -130,16 +130,16 @@ def cpu_reference_run(cfg: int, sample_rows: int, steps: int, threads: int):
                                        n_supp=w.n_supp, datekeys=w.dims["date"][0]))
         else:
             fact.append(np.zeros(sample_rows, np.int32))
-    rates, opens = [], []
+    rates, opens, result = [], [], None
     for _ in range(steps):
-        _, stats = oracle.run_workload(w, "port", threads=threads, fact=fact)
+        result, stats = oracle.run_workload(w, "port", threads=threads, fact=fact)
         rates.append(sample_rows / (stats.compute_ms / 1e3))
         opens.append(stats.open_ms)
     desc = (f"{sample_rows} fact rows (rows 0..{sample_rows - 1}) of config {cfg}, tuple_per_bulk "
             f"{w.tuple_per_bulk}, generated host loop compiled by g++ -O2 (key bytes hashed as signed char), "
             f"{threads} worker threads; pipeline compute time (transform + reduce), hash build excluded "
             f"({statistics.median(opens):.0f} ms)")
-    return rates, statistics.median(opens), desc
+    return rates, statistics.median(opens), desc, result
 
 
 def default_cpu_sample(cfg: int, threads: int) -> int:
@@ -159,7 +159,7 @@ def reference_arm(args):
     for _ in range(max(0, args.warmup - 1)):
         cpu_reference_run(args.config, sample, 1, threads)
     t0 = time.time()
-    rates, _, desc = cpu_reference_run(args.config, sample, args.steps, threads)
+    rates, _, desc, _ = cpu_reference_run(args.config, sample, args.steps, threads)
     wall = time.time() - t0
     v = statistics.median(rates)
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
@@ -343,13 +343,28 @@ def ours_arm(args):
                "api": "svm_object_put (pinned host columns) + svm_run_pipeline + svm_object_read"}
         eng.drop("lineorder_e2e")
 
-    cpu = None
+    cpu, parity = None, None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        sample = args.cpu_sample_rows or default_cpu_sample(args.config, threads)
-        rates, _, desc = cpu_reference_run(args.config, sample, 3, threads)
+        sample = min(rows, args.cpu_sample_rows or default_cpu_sample(args.config, threads))
+        rates, _, desc, (pk, ps) = cpu_reference_run(args.config, sample, 3, threads)
         cpu = {"value": statistics.median(rates), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": desc}
+        # Parity at full dimension sizes: the same query on the GPU over a view
+        # of the same fact rows the port just ran, compared bit for bit.
+        import copy
+        qp = copy.deepcopy(w.query)
+        qp.id = w.query.id + "_parity"
+        qp.pre_pipeline_id[0] = "lineorder_parity"
+        eng.view("lineorder_parity", "lineorder", 0, sample)
+        eng.run(qp)
+        gk, gs = eng.result(qp.id, w.key_num)
+        parity = {"rows": sample, "groups": int(len(gs)), "equal": bool(np.array_equal(gk, pk) and
+                                                                         np.array_equal(gs, ps)),
+                  "against": "oracle port (the reference's generated CPU path) on the same fact rows, "
+                             "full-size dimensions, REF_COMPAT; int64 sums and key rows compared bit for bit"}
+        eng.drop(qp.id)
+        eng.drop("lineorder_parity")
 
     batched = None
     if args.config == 2 and not args.no_batched:
@@ -371,7 +386,7 @@ def ours_arm(args):
                               rows_per_gpu=rows, parallelism=f"row shards x{world}"),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                "clocks": clk, "dimension_build_s": build_s,
-               "hbm_frac_of_measured": roofline["frac"], "batched": batched}
+               "hbm_frac_of_measured": roofline["frac"], "parity": parity, "batched": batched}
         print(json.dumps(out))
     eng.close()
     if world > 1:

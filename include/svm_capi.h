@@ -240,9 +240,15 @@ svm_status svm_pipeline_footprint(svm_ctx* ctx, const svm_pipeline* pipe, unsign
  * is rejected with SVM_E_INVALID_ARG.  The array is shared by all calls and
  * keeps the last call's contents; each call clears what must start at zero.
  * Calls whose work overlaps on the GPU (two host threads, or two contexts on
- * one device) race on it: serialise them.  The first call on a device looks
- * the array up (cudaGetSymbolAddress) with that device current; make that
- * first call before any stream capture.  The call is synchronous on the
+ * one device) race on it: serialise them.  svm_init looks the array up
+ * (cudaGetSymbolAddress, with the context's device current; under lazy
+ * module loading that is when the driver places the array), so query calls
+ * only read the cached address; were it missing, the first call would look
+ * it up itself, and that call should then come before any stream capture.
+ * Errors: a key outside [key_min, key_max] is SVM_E_DEVICE, a device wait
+ * that gave up SVM_E_TIMEOUT (both reported before the row count is
+ * compared with max_rows); more groups than max_rows, or max_rows 0 for a
+ * query without keys, is SVM_E_INVALID_ARG.  The call is synchronous on the
  * context's stream.
  *
  * Inputs: cols[c] int32 device pointers, 16-byte aligned, readable up to
@@ -273,6 +279,17 @@ typedef struct svm_noalloc_scan {
 svm_status svm_scan_aggregate_noalloc(svm_ctx* ctx, const svm_noalloc_scan* q, int32_t* const* key_out,
                                       long long* const* sum_out, unsigned long long max_rows,
                                       unsigned long long* nrows_out);
+
+/* ---- test hook ----------------------------------------------------------------
+ * No counterpart in the reference.  Every wait of the fused scan kernel on an
+ * mbarrier (the copy warp waiting for a free stage, a consumer warp waiting
+ * for its tile) gives up after a number of polls, raises SVM_E_TIMEOUT and
+ * exits, instead of hanging the GPU.  This sets that limit for the context's
+ * later scans (wait_polls; 0 restores the default of 2^22 polls) and, with
+ * stall_copies != 0, makes the copy warp issue no copies, so that every
+ * consumer wait runs out: tests use it to check that the timeout is reported
+ * and that the context stays usable afterwards. */
+svm_status svm_test_device_wait(svm_ctx* ctx, unsigned int wait_polls, int stall_copies);
 
 /* ---- profiling -------------------------------------------------------------- */
 /* With profiling on, the library brackets each of its kernel launches with

@@ -36,7 +36,9 @@ from . import codegen
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF = os.path.join(HERE, "_ref")
-REFERENCE_TREE = os.environ.get("SVM_REFERENCE_DIR", "/root/reference")
+# The reference source tree: SVM_REFERENCE_DIR, else a directory named
+# "reference" beside the repository.
+REFERENCE_TREE = os.environ.get("SVM_REFERENCE_DIR") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 _lock = threading.Lock()
 _libs: dict[str, ctypes.CDLL] = {}

@@ -1,7 +1,8 @@
 #!/usr/bin/env bash
 # ORACLE (test infrastructure only).  Builds the reference-side checker into
-# oracle/_ref/ from the reference sources where they lie (REF, default
-# /root/reference); nothing from the reference tree is copied into the repo.
+# oracle/_ref/ from the reference sources where they lie (SVM_REFERENCE_DIR,
+# default: a directory named "reference" beside the repository); nothing from
+# the reference tree is copied into the repo.
 #
 #   oracle/_ref/ref_codegen          the reference's own CodeGen (codegen/codegen.cpp,
 #                                    codegen/template.cpp) behind oracle/ref_codegen_shim.cpp
@@ -13,8 +14,8 @@
 # clang replaced by g++) against the same headers, into oracle/_ref/q/.
 # The reference runtime header includes <xmmintrin.h>, so this builds on x86 only.
 set -euo pipefail
-REF="${SVM_REFERENCE_DIR:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${SVM_REFERENCE_DIR:-$HERE/../../reference}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/codegen/codegen.cpp" ]; then
   echo "build_ref.sh: reference tree not found at $REF" >&2

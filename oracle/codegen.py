@@ -7,7 +7,7 @@ on the CPU -- so that text can be compiled (g++) and run by ``oracle/driver.cpp`
 against either this repository's runtime restatement (``svm_port_runtime.h``)
 or the reference's own runtime headers (``oracle/_ref``).  Each function below
 names the reference function it follows.  The emitted text is meant to be
-character-identical to the reference's; ``tests/test_oracle_codegen.py`` checks
+character-identical to the reference's; ``tests/test_oracle.py`` checks
 that against the reference's own CodeGen compiled here (``oracle/ref_codegen_shim.cpp``).
 
 Only the product's tests, ``bench.py``'s CPU legs and ``__graft_entry__.smoke``

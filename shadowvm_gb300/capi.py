@@ -117,6 +117,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "svm_profile_reset": (I, [P]),
         "svm_profile_read": (I, [P, I, ctypes.POINTER(U64), ctypes.POINTER(D)]),
         "svm_kernel_launches": (U64, []),
+        "svm_test_device_wait": (I, [P, ctypes.c_uint, I]),
         "svm_scan_aggregate_noalloc": (I, [P, ctypes.POINTER(svm_noalloc_scan), ctypes.POINTER(P),
                                            ctypes.POINTER(P), U64, ctypes.POINTER(U64)]),
     }

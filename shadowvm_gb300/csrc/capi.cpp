@@ -271,7 +271,7 @@ svm_status svm_init(const svm_config* cfg, svm_ctx** out) {
   x->device = c.device;
   if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMalloc(&x->d_error, sizeof(int)) != cudaSuccess ||
-      cudaMemset(x->d_error, 0, sizeof(int)) != cudaSuccess) {
+      cudaMemset(x->d_error, 0, sizeof(int)) != cudaSuccess || svm::noalloc_prepare(x) != SVM_OK) {
     delete h;
     return SVM_E_CUDA;
   }
@@ -711,6 +711,15 @@ svm_status svm_pipeline_footprint(svm_ctx* c, const svm_pipeline* p, unsigned lo
 }
 
 unsigned long long svm_kernel_launches(void) { return svm::launches_total(); }
+
+svm_status svm_test_device_wait(svm_ctx* c, unsigned int wait_polls, int stall_copies) {
+  if (!c) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  x->wait_polls = wait_polls;
+  x->stall_copies = stall_copies != 0;
+  return SVM_OK;
+}
 
 svm_status svm_profile_enable(svm_ctx* c, int on) {
   if (!c) return SVM_E_INVALID_ARG;

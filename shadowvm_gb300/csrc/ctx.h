@@ -158,6 +158,10 @@ struct Ctx {
   std::map<std::string, std::tuple<int, bool, int>> star_tune;
   void purge_rank_cache();  // entries whose code storage no object uses any more
   int* d_error = nullptr;                     // device error word
+  // Test hook (svm_test_device_wait): the fused scan's mbarrier poll limit
+  // (0 = default) and whether its copy warp issues no copies.
+  uint32_t wait_polls = 0;
+  int stall_copies = 0;
   // Grow-only scratch arena, carved per operation.
   DevBufPtr scratch;
   size_t scratch_used = 0;
@@ -198,6 +202,22 @@ struct Ctx {
   void prof_end(int cls, cudaEvent_t a);
   void prof_collect();
 };
+
+// The status and message for a kernel's error word (a DevError code).
+inline svm_status device_error_status(int code, const char** msg) {
+  switch (code) {
+    case DERR_DIV0: *msg = "integer division by zero in an expression"; return SVM_E_DEVICE;
+    case DERR_HASH_FULL: *msg = "dimension hash table overflow"; return SVM_E_DEVICE;
+    case DERR_KEY_RANGE: *msg = "group key outside its computed range"; return SVM_E_DEVICE;
+    case DERR_TIMEOUT: *msg = "a bounded device wait gave up (the kernel exited early)"; return SVM_E_TIMEOUT;
+    case DERR_LOAD_ITEM: *msg = "an item longer than 4095 bytes"; return SVM_E_INVALID_ARG;
+    default: *msg = "the kernel reported an error"; return SVM_E_DEVICE;
+  }
+}
+
+// The allocation-free scan's static scratch, looked up for x->device
+// (kern_noalloc.cu); svm_init calls it once per context.
+svm_status noalloc_prepare(Ctx* x);
 
 // Pipelines (pipeline.cpp).
 svm_status run_pipeline(Ctx* ctx, const svm_pipeline* p);

@@ -8,10 +8,6 @@
 
 namespace svm {
 
-// Error codes a kernel may raise in StarParams::error / SelectParams::error.
-enum DevError : int { DERR_NONE = 0, DERR_DIV0 = 1, DERR_HASH_FULL = 2, DERR_KEY_RANGE = 3,
-                      DERR_TIMEOUT = 4, DERR_LOAD_ITEM = 5 };
-
 // ---------------------------------------------------------------- mbarrier / bulk copy (PTX)
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);

@@ -27,6 +27,8 @@
 // Items convert as strtol(s, NULL, 10) on LP64 -- leading isspace, optional
 // sign, decimal digits, clamp to the 64-bit range on overflow -- then Int32
 // columns keep the low 32 bits (atoi), Int64 columns the value (atol).
+#include <atomic>
+
 #include "kern_common.cuh"
 #include "kernels.h"
 
@@ -433,18 +435,21 @@ __global__ void __launch_bounds__(kWarps * 32) load_parse_kernel(const uint8_t* 
 }
 
 template <typename K>
-int grid_for(K kernel, int* per_sm, unsigned long long spans) {
-  if (!*per_sm) {
-    int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kWarps * 32, 0) != cudaSuccess || b < 1) b = 1;
-    *per_sm = b;
+int grid_for(K kernel, std::atomic<int>* per_sm_cache, unsigned long long spans) {
+  // Blocks per SM depend on the kernel and the architecture only; a race
+  // between threads computes the same value twice.
+  int per_sm = per_sm_cache->load(std::memory_order_relaxed);
+  if (!per_sm) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarps * 32, 0) != cudaSuccess || per_sm < 1)
+      per_sm = 1;
+    per_sm_cache->store(per_sm, std::memory_order_relaxed);
   }
   const unsigned long long want = (spans + kWarps - 1) / kWarps;
-  const unsigned long long cap = (unsigned long long)num_sms() * *per_sm;
+  const unsigned long long cap = (unsigned long long)num_sms() * per_sm;
   return (int)(want < 1 ? 1 : want < cap ? want : cap);
 }
 
-int summary_per_sm = 0, parse_per_sm[2] = {0, 0};
+std::atomic<int> summary_per_sm{0}, parse_per_sm[2] = {{0}, {0}};
 
 }  // namespace
 

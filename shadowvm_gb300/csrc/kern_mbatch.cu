@@ -532,11 +532,7 @@ size_t mbatch_smem_bytes(const BatchParams& b) {
 }
 
 int mbatch_grid_size(const BatchParams& b, size_t smem) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(mbatch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024);
-    attr = true;
-  }
+  allow_dynamic_smem(reinterpret_cast<const void*>(&mbatch_kernel), 226 * 1024);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mbatch_kernel, kMBThreads, smem);
   return num_sms() * per_sm;

@@ -20,18 +20,19 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 unsigned long long* g_scratch_addr[kMaxDevices] = {};
 
-// The array's device address for the current device.  In host code
+// The array's device address on device `dev`.  In host code
 // `g_noalloc_scratch` names a host-side stand-in, not device memory, so the
 // address is looked up once per device, with that device current.
-svm_status scratch_address(Ctx* x, unsigned long long** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e) return x->cuda_fail(e, "cudaGetDevice");
+// svm_init does it for its context's device; a later call only reads it.
+svm_status scratch_address(Ctx* x, int dev, unsigned long long** out) {
   if (dev < 0 || dev >= kMaxDevices) return x->fail(SVM_E_INVALID_ARG, "device ordinal out of range");
   std::lock_guard<std::mutex> g(g_mu);
   if (!g_scratch_addr[dev]) {
+    int cur = -1;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (!e && cur != dev) e = cudaSetDevice(dev);
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (!e) e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) return x->cuda_fail(e ? e : cudaErrorInvalidSymbol, "cudaGetSymbolAddress");
     g_scratch_addr[dev] = static_cast<unsigned long long*>(p);
   }
@@ -40,6 +41,15 @@ svm_status scratch_address(Ctx* x, unsigned long long** out) {
 }
 
 }  // namespace
+
+// Called by svm_init with the context's device current: looks the static
+// scratch up once per device, so that no query-path call loads the module
+// (which, under lazy module loading, is when the driver places the array).
+svm_status noalloc_prepare(Ctx* x) {
+  unsigned long long* p;
+  return scratch_address(x, x->device, &p);
+}
+
 }  // namespace svm
 
 using namespace svm;
@@ -126,8 +136,10 @@ extern "C" svm_status svm_scan_aggregate_noalloc(svm_ctx* c, const svm_noalloc_s
     return x->fail(SVM_E_INVALID_ARG, "noalloc scan: " + std::to_string(G) + " groups x " + std::to_string(nm) +
                                           " metrics need " + std::to_string(need) + " scratch words; the static "
                                           "scratch holds " + std::to_string(SVM_NOALLOC_SCRATCH_WORDS));
+  if (nkeys == 0 && q->nrows > 0 && max_rows < 1)
+    return x->fail(SVM_E_INVALID_ARG, "noalloc scan: max_rows is 0 but a query without keys writes one row");
   unsigned long long* scratch;
-  svm_status st = scratch_address(x, &scratch);
+  svm_status st = scratch_address(x, x->device, &scratch);
   if (st) return st;
   if (q->nrows == 0) return SVM_OK;  // no rows: no bulk, no result row
 
@@ -165,6 +177,15 @@ extern "C" svm_status svm_scan_aggregate_noalloc(svm_ctx* c, const svm_noalloc_s
   if (!e) e = launch_star(P, star_grid_size(P, smem), star_block_size(), smem, x->stream);
   if (e) return x->cuda_fail(e, "noalloc scan");
   unsigned long long rows = 0;
+  // The kernel's error word is read before the result is used: a key outside
+  // its range or a wait that gave up is reported as such, not as a row count.
+  auto device_error = [&](int h) {
+    const char* m;
+    const svm_status s = device_error_status(h, &m);
+    return x->fail(s, std::string("noalloc scan: ") +
+                          (h == DERR_KEY_RANGE ? "a key value lies outside [key_min, key_max]" : m));
+  };
+  int h = 0;
   if (nkeys == 0) {
     for (int m = 0; m < nm && !e; m++)
       e = cudaMemcpyAsync(sum_out[m], P.sums + m, 8, cudaMemcpyDeviceToDevice, x->stream);
@@ -173,8 +194,10 @@ extern "C" svm_status svm_scan_aggregate_noalloc(svm_ctx* c, const svm_noalloc_s
     e = launch_finalize_dense(P, nullptr, nullptr, nullptr, fin, scant, nullptr, x->stream);
     unsigned long long* pos = fin + (G + 1) / 2 + 1;
     if (!e) e = cudaMemcpyAsync(&rows, pos + G, 8, cudaMemcpyDeviceToHost, x->stream);
+    if (!e) e = cudaMemcpyAsync(&h, P.error, sizeof(int), cudaMemcpyDeviceToHost, x->stream);
     if (!e) e = cudaStreamSynchronize(x->stream);
     if (e) return x->cuda_fail(e, "noalloc scan");
+    if (h) return device_error(h);
     if (rows > max_rows)
       return x->fail(SVM_E_INVALID_ARG, "noalloc scan: " + std::to_string(rows) + " result rows exceed max_rows " +
                                             std::to_string(max_rows));
@@ -183,12 +206,10 @@ extern "C" svm_status svm_scan_aggregate_noalloc(svm_ctx* c, const svm_noalloc_s
     for (int m = 0; m < nm; m++) mo[m] = sum_out[m];
     e = launch_finalize_dense(P, key_out, mo, wide, fin, scant, nullptr, x->stream);
   }
-  int h = 0;
   if (!e) e = cudaMemcpyAsync(&h, P.error, sizeof(int), cudaMemcpyDeviceToHost, x->stream);
   if (!e) e = cudaStreamSynchronize(x->stream);
   if (e) return x->cuda_fail(e, "noalloc scan");
-  if (h) return x->fail(SVM_E_DEVICE, h == 3 ? "noalloc scan: a key value lies outside [key_min, key_max]"
-                                             : "noalloc scan: the kernel reported an error");
+  if (h) return device_error(h);
   *nrows_out = rows;
   return SVM_OK;
 }

@@ -409,16 +409,17 @@ __global__ void __launch_bounds__(kStarThreads, 3) star_kernel(const __grid_cons
   const long long a0 = P.row_begin & ~3ll;
   const long long end4 = (P.row_end + 3) & ~3ll;  // copies stop at the 4-row boundary past row_end
   const long long ntiles = (P.row_end - a0 + kTileRows - 1) / kTileRows;
+  const uint32_t polls = P.wait_polls ? P.wait_polls : kWaitPolls;
   long long acc[kMaxMetrics + 1] = {0, 0, 0, 0};
 
   if (warp == kConsumerWarps) {
     // ---------------- producer: one lane issues the bulk copies
-    if (lane == 0) {
+    if (lane == 0 && !P.stall_copies) {
       long long issued = 0;
       for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, issued++) {
         int s = (int)(issued % nst);
         long long k = issued / nst;
-        if (k > 0 && !mbar_wait_bounded(&S.empty[s], (uint32_t)((k - 1) & 1), kWaitPolls)) {
+        if (k > 0 && !mbar_wait_bounded(&S.empty[s], (uint32_t)((k - 1) & 1), polls)) {
           raise_error(P.error, DERR_TIMEOUT);
           break;
         }
@@ -432,7 +433,7 @@ __global__ void __launch_bounds__(kStarThreads, 3) star_kernel(const __grid_cons
       // Every issued copy lands before the block exits.
       long long first = issued > nst ? issued - nst : 0;
       for (long long q = first; q < issued; q++)
-        mbar_wait_bounded(&S.full[q % nst], (uint32_t)((q / nst) & 1), kWaitPolls);
+        mbar_wait_bounded(&S.full[q % nst], (uint32_t)((q / nst) & 1), polls);
     }
   } else {
     // ---------------- consumers
@@ -443,7 +444,7 @@ __global__ void __launch_bounds__(kStarThreads, 3) star_kernel(const __grid_cons
     long long i = 0;
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
       int s = (int)(i % nst);
-      if (!mbar_wait_bounded(&S.full[s], (uint32_t)((i / nst) & 1), kWaitPolls)) {
+      if (!mbar_wait_bounded(&S.full[s], (uint32_t)((i / nst) & 1), polls)) {
         raise_error(P.error, DERR_TIMEOUT);
         break;
       }
@@ -578,14 +579,9 @@ static const void* star_entry_t(int agg) {
 }
 
 int star_blocks_per_sm(const StarParams& p, size_t smem) {
-  static bool attr_set[6] = {false, false, false, false, false, false};
   const bool prog = plan_needs_prog(p);
-  int a = (p.agg == AGG_SCALAR ? 0 : p.agg == AGG_DENSE_SMEM ? 1 : 2) + (prog ? 3 : 0);
   const void* fn = prog ? star_entry_t<true>(p.agg) : star_entry_t<false>(p.agg);
-  if (!attr_set[a]) {
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024);
-    attr_set[a] = true;
-  }
+  allow_dynamic_smem(fn, 210 * 1024);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kStarThreads, smem);
   return per_sm;
@@ -811,11 +807,7 @@ size_t batch_smem_bytes(const BatchParams& b) {
 }
 
 int batch_grid_size(const BatchParams& b, size_t smem) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024);
-    attr = true;
-  }
+  allow_dynamic_smem(reinterpret_cast<const void*>(&batch_kernel), 210 * 1024);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, kStarThreads, smem);
   return num_sms() * (per_sm < 1 ? 1 : per_sm);

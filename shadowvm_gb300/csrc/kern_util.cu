@@ -1,6 +1,9 @@
 // Utility kernels: seeded data generation, column min/max, prefix scans.
 #include <atomic>
 #include <climits>
+#include <mutex>
+#include <set>
+#include <tuple>
 
 #include "kern_common.cuh"
 #include "kernels.h"
@@ -11,15 +14,40 @@ static std::atomic<unsigned long long> g_launches{0};
 void note_launch(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 unsigned long long launches_total() { return g_launches.load(); }
 
+// Per-device caches: the current device's SM count, and the dynamic
+// shared-memory limit raised once per (device, kernel), since a function
+// attribute applies only to the device that was current when it was set.
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_dev_mu;
+int g_sms[kMaxDevices] = {};
+std::set<std::tuple<int, const void*, int>> g_smem_attr;
+
+int current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+  return dev;
+}
+}  // namespace
+
 int num_sms() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
+  const int dev = current_device();
+  std::lock_guard<std::mutex> g(g_dev_mu);
+  if (!g_sms[dev]) {
+    int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
+    g_sms[dev] = sms > 0 ? sms : 1;
   }
-  return sms;
+  return g_sms[dev];
+}
+
+cudaError_t allow_dynamic_smem(const void* fn, int bytes) {
+  const int dev = current_device();
+  std::lock_guard<std::mutex> g(g_dev_mu);
+  if (g_smem_attr.count(std::make_tuple(dev, fn, bytes))) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) g_smem_attr.insert(std::make_tuple(dev, fn, bytes));
+  return e;
 }
 
 // ---------------------------------------------------------------- generation

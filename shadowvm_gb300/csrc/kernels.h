@@ -9,7 +9,11 @@
 
 namespace svm {
 
+// SM count of the current device (cached per device).
 int num_sms();
+// Raises `fn`'s dynamic shared-memory limit to `bytes` on the current device
+// (once per device and kernel; thread-safe).
+cudaError_t allow_dynamic_smem(const void* fn, int bytes);
 // Process-wide count of kernel launches (every <<<>>> site calls this).
 void note_launch(int n = 1);
 unsigned long long launches_total();

@@ -133,10 +133,9 @@ svm_status sync_and_check(Ctx* x, const char* what) {
   if (e) return x->cuda_fail(e, what);
   if (h) {
     cudaMemset(x->d_error, 0, sizeof(int));
-    const char* m = h == 1 ? "integer division by zero in an expression"
-                           : h == 2 ? "dimension hash table overflow"
-                                    : "group key outside its computed range";
-    return x->fail(SVM_E_DEVICE, std::string(what) + ": " + m);
+    const char* m;
+    const svm_status s = device_error_status(h, &m);
+    return x->fail(s, std::string(what) + ": " + m);
   }
   return SVM_OK;
 }
@@ -605,6 +604,8 @@ svm_status plan_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::ve
   StarParams& P = plan->P;
   P = StarParams{};
   P.error = x->d_error;
+  P.wait_polls = x->wait_polls;
+  P.stall_copies = x->stall_copies;
   P.row_begin = (long long)src->row0;
   P.row_end = (long long)(src->row0 + src->nrows);
   std::vector<int>& fact_cols = plan->fact_cols;  // StarParams::cols slot -> fact column

@@ -18,6 +18,12 @@ constexpr int kSmemTableBytes = 64 * 1024;  // dimension tables staged in shared
 constexpr int kSmemAggBytes = 64 * 1024;    // per-block group table in shared memory
 constexpr int kHashRate = 5;       // com/cpp/define.hpp:29
 
+// ---------------------------------------------------------------- device errors
+// Error codes a kernel may raise in its error word (StarParams::error,
+// SelectParams::error, ...); the first one raised is kept.
+enum DevError : int { DERR_NONE = 0, DERR_DIV0 = 1, DERR_HASH_FULL = 2, DERR_KEY_RANGE = 3,
+                      DERR_TIMEOUT = 4, DERR_LOAD_ITEM = 5 };
+
 // ---------------------------------------------------------------- expressions
 // Stack-machine bytecode for int32 C expressions (wrapping arithmetic, C
 // truncating division, comparisons yield 0/1, && || short-circuit).
@@ -163,6 +169,11 @@ struct StarParams {
   unsigned long long* hkeys;        // AGG_HASH_GLOBAL: packed keys per slot (~0 = empty)
   int smem_table_words;             // words of dimension tables staged in shared memory
   int* error;                       // device error word (division by zero, hash overflow)
+  // Bounded waits: polls of an mbarrier before the kernel gives up with
+  // DERR_TIMEOUT (0: the default, 2^22).  stall_copies != 0 (a test hook)
+  // makes the copy warp issue nothing, so every consumer wait runs out.
+  uint32_t wait_polls;
+  int stall_copies;
   // Deferred aggregation (plans without bytecode): a surviving row's operand
   // words -- the probe words and fact values its keys and metrics read -- are
   // appended to a per-warp buffer and aggregated 32 rows at a time.

@@ -230,6 +230,11 @@ class Engine:
         return keys, mets
 
     # ------------------------------------------------------------ profiling
+    def test_device_wait(self, wait_polls: int = 0, stall_copies: bool = False):
+        """Test hook: the fused scan's mbarrier poll limit (0 = default) and
+        whether its copy warp issues no copies (svm_test_device_wait)."""
+        self._check(self.lib.svm_test_device_wait(self.h, wait_polls, int(stall_copies)))
+
     def profile(self, on: bool = True):
         self._check(self.lib.svm_profile_enable(self.h, int(on)))
 

@@ -321,18 +321,6 @@ def load_batch(engine, bw: BatchWorkload, generate_on_device: bool = True, build
             engine.run(p)
 
 
-def exact_batch_query(bw: BatchWorkload, i: int, fact: list | None = None):
-    """One query of the batch through the NumPy evaluator (oracle side)."""
-    from oracle import sql_exact
-    q = bw.queries[i]
-    objs = {name: list(cols) for name, cols in bw.fact.dims.items()}
-    for p in bw.dim_pipelines:
-        if p.id in q.pipe.pre_pipeline_id:
-            objs[p.id] = sql_exact.run_select(p, objs[p.pre_pipeline_id[0]])
-    f = bw.fact.fact_host(q.row0, q.nrows) if fact is None else [c[q.row0:q.row0 + q.nrows] for c in fact]
-    return sql_exact.run_reduce(q.pipe, f, [objs[x] for x in q.pipe.pre_pipeline_id[1:]])
-
-
 # ------------------------------------------------------------------ GPU side
 def gen_fact_on_device(engine, w: Workload, fact_id: str = "lineorder", row0: int = 0):
     """Rows row0 .. row0 + w.fact_rows - 1 of the workload's fact table,

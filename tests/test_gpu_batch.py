@@ -5,6 +5,7 @@ parity tests pin to the reference), and in EXACT mode the NumPy evaluation."""
 import numpy as np
 import pytest
 
+from oracle_helpers import exact_batch_query
 from shadowvm_gb300 import workloads as W
 from shadowvm_gb300.pipeline import dim_pipeline, fact_pipeline
 from shadowvm_gb300.proto import ValType
@@ -58,7 +59,7 @@ def test_batch_exact_equals_numpy(engine_factory):
     got = batched(eng, bw)
     fact = bw.fact.fact_host(0, bw.fact.fact_rows)
     for i in range(len(bw.queries)):
-        ek, es = W.exact_batch_query(bw, i, fact)
+        ek, es = exact_batch_query(bw, i, fact)
         np.testing.assert_array_equal(got[i][0], ek, err_msg=f"keys of query {i}")
         np.testing.assert_array_equal(got[i][1], es, err_msg=f"sums of query {i}")
 

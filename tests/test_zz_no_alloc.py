@@ -5,8 +5,11 @@ It exists for callers that cannot allocate device memory on their query path
 must not take cudaMalloc's implicit device-wide synchronisation).  Its scratch
 is a static device array shared by every call, so this checks, through the C
 ABI, that two calls in a row each give exactly the rows svm_run_pipeline gives
-for the equivalent Filter/ReduceBy pipeline (integer sums: bit-exact), and
-that a query too large for the array is refused.  The test's own buffers are
+for the equivalent Filter/ReduceBy pipeline (integer sums: bit-exact), that a
+grouped call equals an independent NumPy group-by, that a query too large for
+the array is refused, and that its error paths (a key outside its declared
+range, too few output rows, an unaligned column) report their own status and
+leave the shared scratch usable.  The test's own buffers are
 allocated by the test, never by the entry point.
 
 This file is collected last so that a failure here comes after every other test.
@@ -106,3 +109,49 @@ def test_noalloc_rejects_groups_beyond_the_static_scratch(table):
         noalloc(eng, ptrs, n, [], [(3, 0, 999_999)], [(capi.METRIC_COL, 1, 1)], max_rows=1)
     assert e.value.status == capi.E_INVALID_ARG
     assert "scratch" in e.value.message
+
+
+def test_noalloc_grouped_matches_numpy(table):
+    """The same grouped query against an independent NumPy group-by of the
+    host columns (the C semantics: int32 products wrap, sums are int64)."""
+    eng, ptrs, n = table
+    cols = [eng.read("nf", c).astype(np.int64) for c in range(4)]
+    keep = (cols[0] >= 5) & (cols[0] <= 45) & (cols[3] <= 700_000)
+    k0, k1 = cols[2][keep], cols[0][keep]
+    prod = ((cols[3][keep] * cols[1][keep]) & 0xFFFFFFFF).astype(np.uint32).astype(np.int32).astype(np.int64)
+    uniq, inv = np.unique(np.stack([k0, k1], axis=1), axis=0, return_inverse=True)
+    inv = inv.reshape(-1)
+    want = np.zeros((len(uniq), 2), np.int64)
+    np.add.at(want[:, 0], inv, prod)
+    np.add.at(want[:, 1], inv, cols[1][keep])
+    k, s = noalloc(eng, ptrs, n, [(0, 5, 45), (3, -2**31, 700_000)], [(2, 0, 6), (0, 0, 49)],
+                   [(capi.METRIC_MUL, 3, 1), (capi.METRIC_COL, 1, 1)], max_rows=7 * 50)
+    np.testing.assert_array_equal(k, uniq.astype(np.int32))
+    np.testing.assert_array_equal(s, want)
+
+
+def test_noalloc_error_paths(table):
+    eng, ptrs, n = table
+    # a key value outside [key_min, key_max] (column 2 holds 0..6): a device error
+    with pytest.raises(capi.SvmError) as e:
+        noalloc(eng, ptrs, n, [], [(2, 0, 5)], [(capi.METRIC_COL, 1, 1)], max_rows=64)
+    assert e.value.status == capi.E_DEVICE and "key" in e.value.message
+    # more groups than max_rows
+    with pytest.raises(capi.SvmError) as e:
+        noalloc(eng, ptrs, n, [], [(2, 0, 6)], [(capi.METRIC_COL, 1, 1)], max_rows=6)
+    assert e.value.status == capi.E_INVALID_ARG and "max_rows" in e.value.message
+    # a query without keys writes one row: max_rows 0 is refused before any launch
+    with pytest.raises(capi.SvmError) as e:
+        noalloc(eng, ptrs, n, [], [], [(capi.METRIC_COL, 1, 1)], max_rows=0)
+    assert e.value.status == capi.E_INVALID_ARG
+    # a column pointer that is not 16-byte aligned
+    bad = list(ptrs)
+    bad[1] = ptrs[1] + 4
+    with pytest.raises(capi.SvmError) as e:
+        noalloc(eng, bad, n - 1, [], [(2, 0, 6)], [(capi.METRIC_COL, 1, 1)], max_rows=64)
+    assert e.value.status == capi.E_INVALID_ARG and "aligned" in e.value.message
+    # the shared scratch keeps no error from the failed calls
+    k, s = noalloc(eng, ptrs, n, [], [(2, 0, 6)], [(capi.METRIC_COL, 1, 1)], max_rows=64)
+    c1, c2 = eng.read("nf", 1).astype(np.int64), eng.read("nf", 2)
+    np.testing.assert_array_equal(k[:, 0], np.arange(7, dtype=np.int32))
+    np.testing.assert_array_equal(s[:, 0], np.array([c1[c2 == v].sum() for v in range(7)], np.int64))
