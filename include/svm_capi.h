@@ -280,6 +280,24 @@ svm_status svm_scan_aggregate_noalloc(svm_ctx* ctx, const svm_noalloc_scan* q, i
                                       long long* const* sum_out, unsigned long long max_rows,
                                       unsigned long long* nrows_out);
 
+/* Narrows the fused scan's launch configurations for the context's later
+ * queries: rows_per_lane -1 (any), 0 (the interpreted kernel) or 4 / 8 (the
+ * kernel compiled for the plan's shape, with that many rows per consumer
+ * lane); ring_stages 0 (any) or 2..4; tables_staged -1 (any), 0 (small
+ * dimension tables probed in L2) or 1 (staged in shared memory).  The rule,
+ * or with svm_config.autotune the tuner, picks among the configurations
+ * left; a query none fits returns SVM_E_UNSUPPORTED.  Every configuration
+ * computes the same result.  No counterpart in the reference (its launch is
+ * fixed at 1024 threads a block, com/cpp/com.cu:19-20). */
+svm_status svm_pin_launch(svm_ctx* ctx, int rows_per_lane, int ring_stages, int tables_staged);
+
+/* The launch configuration of the context's last fused scan (the kernel
+ * compiled for the plan's shape or the interpreted one, rows per consumer
+ * lane, ring stages, table placement, the steps in order, grid and shared
+ * memory), as a JSON object in `buf` (cut to cap - 1 bytes, NUL-terminated;
+ * empty before the first scan).  No counterpart in the reference. */
+svm_status svm_last_launch(svm_ctx* ctx, char* buf, unsigned long long cap);
+
 /* ---- test hook ----------------------------------------------------------------
  * No counterpart in the reference.  Every wait of the fused scan kernel on an
  * mbarrier (the copy warp waiting for a free stage, a consumer warp waiting

@@ -346,6 +346,36 @@ def run_workload(w, mode: str = "port", threads: int = 1, fact: list | None = No
     return merge_groups(sink, w.key_num, w.metric_num), stats
 
 
+def run_workload_rows(w, mode: str = "port", threads: int = 1, fact: list | None = None):
+    """A workload whose fact pipeline has no ReduceBy (a joined projection):
+    its output columns, rows in order bulk by bulk as the reference's
+    TransformTask writes them (core/pipeline.cu:262-344)."""
+    from shadowvm_gb300.workloads import schema_of
+    tpb = w.tuple_per_bulk
+    objs = {name: Obj.from_columns(cols, schema_of(cols), tpb, mode) for name, cols in w.dims.items()}
+    fact = w.fact_host(0, w.fact_rows) if fact is None else fact
+    objs["lineorder"] = Obj.from_columns(fact, w.fact_schema(), tpb, mode)
+    for p in w.dim_pipelines:
+        out, _ = run_pipeline(p, objs[p.pre_pipeline_id[0]], [], tpb, threads, mode)
+        objs[p.id] = out
+    q = w.query
+    sink, _ = run_pipeline(q, objs[q.pre_pipeline_id[0]], [objs[i] for i in q.pre_pipeline_id[1:]],
+                           tpb, threads, mode)
+    ncols = len([op.output for op in q.workflow if op.type == OpType.Sink][0].column_list)
+    return [sink.concat(c) for c in range(ncols)]
+
+
+def exact_workload_rows(w, fact: list | None = None):
+    """The joined projection through sql_exact (every dimension row joinable)."""
+    from . import sql_exact
+    objs = {name: list(cols) for name, cols in w.dims.items()}
+    for p in w.dim_pipelines:
+        objs[p.id] = sql_exact.run_select(p, objs[p.pre_pipeline_id[0]])
+    q = w.query
+    fact = w.fact_host(0, w.fact_rows) if fact is None else fact
+    return sql_exact.run_join_select(q, fact, [objs[i] for i in q.pre_pipeline_id[1:]])
+
+
 def exact_workload(w, fact: list | None = None):
     """The same workload through sql_exact (every dimension row joinable)."""
     from . import sql_exact

@@ -298,6 +298,31 @@ def run_select(p: PipelineInfo, cols: list[np.ndarray]) -> list[np.ndarray]:
     return res
 
 
+def run_join_select(p: PipelineInfo, fact: list[np.ndarray], dims: list[list[np.ndarray]]) -> list[np.ndarray]:
+    """A Map pipeline with joins (the reference's join block, then its select
+    block, codegen/codegen.cpp:121-180): rows passing the filter whose every
+    join key has a match (the first dimension row with that key), projected
+    in row order."""
+    filt, sel, _, _, joins, _ = _bind(p)
+    n = len(fact[0]) if fact else 0
+    env = {(0, c): _col(v) for c, v in enumerate(fact)}
+    mask = np.ones(n, bool)
+    if filt and n:
+        mask = evaluate(parse("&&".join(filt)), env, n) != 0
+    for lk, rk in joins:
+        lo, lc = _keyref(lk)
+        ro, rc = _keyref(rk)
+        idx = first_match(np.asarray(dims[ro - 1][rc], np.int32), _num(env[(lo, lc)]))
+        mask &= idx >= 0
+        safe = np.where(idx >= 0, idx, 0)
+        for c, col in enumerate(dims[ro - 1]):
+            col = _col(col)
+            env[(ro, c)] = col[safe] if len(col) else np.zeros(n, col.dtype)
+    sub = {k: v[mask] for k, v in env.items()}
+    m = int(mask.sum())
+    return [evaluate(parse(e), sub, m).astype(np.int32) for e in sel]
+
+
 def first_match(dim_keys: np.ndarray, probe: np.ndarray) -> np.ndarray:
     """Index of the first row of dim_keys equal to each probe value, else -1."""
     if len(dim_keys) == 0:

@@ -153,9 +153,24 @@ struct Ctx {
     std::vector<int32_t> hash_of_rank;
   };
   std::map<std::tuple<const void*, const void*, int>, RankCol> rank_cache;
-  // Tuned star launches: plan shape -> (ring depth, tables staged in shared
-  // memory, adjacent L2 probes exchanged at this step or -1).
-  std::map<std::string, std::tuple<int, bool, int>> star_tune;
+  // A launch configuration of the fused scan: ring depth, small tables
+  // staged in shared memory, adjacent L2 probes exchanged at this step (or
+  // -1), and rows per consumer lane of the kernel compiled for the plan's
+  // shape (0: the interpreted kernel).
+  struct StarLaunch {
+    int nst = 2;
+    bool staged = true;
+    int swap = -1;
+    int rows = 0;
+  };
+  // Pinned launch choices (svm_pin_launch): kernel rows per lane (-1: any,
+  // 0: the interpreted kernel, 4 or 8: the compiled one), ring stages (0:
+  // any), tables staged (-1: any).  A pin narrows the candidates; the rule or
+  // the tuner picks among those left.
+  int pin_rows = -1, pin_stages = 0, pin_staged = -1;
+  // Tuned star launches: plan shape -> the fastest configuration measured.
+  std::map<std::string, StarLaunch> star_tune;
+  std::string last_launch;                    // the last fused scan's configuration, as text
   void purge_rank_cache();  // entries whose code storage no object uses any more
   int* d_error = nullptr;                     // device error word
   // Test hook (svm_test_device_wait): the fused scan's mbarrier poll limit

@@ -21,10 +21,25 @@ unsigned long long select_tiles(long long nrows) {
   return (unsigned long long)((nrows + kSelTile - 1) / kSelTile);
 }
 
+// The row's source operands, its conjuncts, then (a join-map pipeline) each
+// join's probe in order -- a row whose key is missing from a table is
+// dropped, as the reference's generated join block clears `cond`
+// (codegen/codegen.cpp:121-149) -- and the joined payload operands.
 __device__ __forceinline__ bool select_row(const SelectParams& p, long long r, int32_t* opnd) {
   for (int c = 0; c < p.ncols_in; c++) opnd[c] = __ldg(p.cols[c] + r);
   for (int k = 0; k < p.npred; k++)
     if (!eval_prog(p.pred[k], opnd, p.error)) return false;
+  if (p.ndims == 0) return true;
+  uint32_t ent[kMaxDims];
+  for (int d = 0; d < p.ndims; d++)
+    if (!probe_dim(p.dims[d], nullptr, opnd[p.join_opnd[d]], ent[d])) return false;
+  for (int k = p.ncols_in; k < p.nopnd; k++) {
+    const Operand o = p.dop[k - p.ncols_in];
+    uint32_t e = ent[0];
+    for (int d = 1; d < kMaxDims; d++)
+      if (o.slot == d) e = ent[d];
+    opnd[k] = payload_value(p.dims[o.slot], o.field, e);
+  }
   return true;
 }
 
@@ -85,7 +100,10 @@ __global__ void select_write_kernel(SelectParams p) {
   for (int k = 0; k < kSelRows; k++) {
     if (!(pass >> k & 1u)) continue;
     long long r = base + k;
-    for (int cc = 0; cc < p.ncols_in; cc++) opnd[cc] = __ldg(p.cols[cc] + r);
+    if (p.ndims)
+      select_row(p, r, opnd);  // the joined operands again (the row passed in the first walk)
+    else
+      for (int cc = 0; cc < p.ncols_in; cc++) opnd[cc] = __ldg(p.cols[cc] + r);
     for (int o = 0; o < p.nout; o++) {
       const Prog& pr = p.proj[o];
       p.out[o][pos] = (pr.n == 1 && pr.op[0] == X_OPND) ? opnd[pr.arg[0]] : eval_prog(pr, opnd, p.error);

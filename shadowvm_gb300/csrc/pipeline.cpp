@@ -161,33 +161,85 @@ ObjectPtr new_result_object(Ctx* x, const std::string& id, const std::vector<int
 }
 
 // ============================================================ select pipelines
-svm_status run_select(Ctx* x, const Bound& b, const ObjectPtr& src) {
-  if (!b.join_rkey.empty())
-    return x->fail(SVM_E_UNSUPPORTED, "JoinWith followed by Map (a join without ReduceBy) is not supported");
+svm_status build_dim(Ctx* x, const ObjectPtr& obj, int key_col, const std::vector<int>& pay_cols,
+                     DimTablePtr* out);
+
+// A Map pipeline, with or without joins.  With JoinWith operators the
+// reference's generated loop probes each joined table after the conjuncts,
+// drops a row whose key is missing, and projects expressions that may read
+// the matched rows of the joined objects (codegen/codegen.cpp:121-180, the
+// select block after the join block; rows written at j, j += cond).  Here
+// the joined objects' tables carry the columns the projections read as
+// payload, and the two-pass order-preserving compaction probes them per row.
+svm_status run_select(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs) {
   if (!b.has_map) return x->fail(SVM_E_UNSUPPORTED, "a pipeline without ReduceBy needs a Map");
   std::string err;
   std::vector<Expr> proj(b.select_exp.size());
-  std::vector<ColRef> opnds;
+  std::vector<ColRef> refs_used;
   for (size_t i = 0; i < b.select_exp.size(); i++) {
     if (!parse_expr(b.select_exp[i], &proj[i], &err))
       return x->fail(err.rfind("unsupported", 0) == 0 ? SVM_E_UNSUPPORTED : SVM_E_INVALID_ARG,
                      "select '" + b.select_exp[i] + "': " + err);
-    collect_refs(proj[i], proj[i].root, &opnds);
+    collect_refs(proj[i], proj[i].root, &refs_used);
   }
   Expr pred;
   bool has_pred = !b.filter_exp.empty();
+  std::vector<ColRef> pred_refs;
   if (has_pred) {
     std::string t = join_filters(b.filter_exp);
     if (!parse_expr(t, &pred, &err))
       return x->fail(err.rfind("unsupported", 0) == 0 ? SVM_E_UNSUPPORTED : SVM_E_INVALID_ARG,
                      "predication '" + t + "': " + err);
-    collect_refs(pred, pred.root, &opnds);
+    collect_refs(pred, pred.root, &pred_refs);
   }
+  // ---- joins: object k (1..n) joined at most once, on an int32 source column
+  const int nref = (int)refs.size();
+  if (nref > kMaxDims) return x->fail(SVM_E_UNSUPPORTED, "more than 4 joined objects");
+  std::vector<int> join_of_obj(nref + 1, -1);
+  for (size_t j = 0; j < b.join_rkey.size(); j++) {
+    ColRef l = b.join_lkey[j], r = b.join_rkey[j];
+    if (r.obj < 1 || r.obj > nref) return x->fail(SVM_E_INVALID_ARG, "rkey names an object the pipeline does not list");
+    if (l.obj != 0) return x->fail(SVM_E_UNSUPPORTED, "lkey must be a column of the source object");
+    if (join_of_obj[r.obj] >= 0) return x->fail(SVM_E_UNSUPPORTED, "an object joined twice");
+    if (l.col < 0 || l.col >= src->ncols || r.col < 0 || r.col >= refs[r.obj - 1]->ncols)
+      return x->fail(SVM_E_INVALID_ARG, "join column out of range");
+    if (src->types[l.col] != SVM_INT32) return x->fail(SVM_E_UNSUPPORTED, "join keys must be int32");
+    join_of_obj[r.obj] = (int)j;
+  }
+  for (auto& r : pred_refs)
+    if (r.obj != 0)
+      return x->fail(SVM_E_UNSUPPORTED, "a Filter on a joined object (the reference evaluates filters before joins)");
+  // Operands: source columns (the projections' and conjuncts' own, then the
+  // join keys), then joined columns as table payload fields.
+  std::vector<ColRef> opnds;
+  auto add_opnd = [&](const ColRef& r) {
+    for (auto& o : opnds)
+      if (o.obj == r.obj && o.col == r.col) return;
+    opnds.push_back(r);
+  };
+  for (auto& r : refs_used)
+    if (r.obj == 0) add_opnd(r);
+  for (auto& r : pred_refs) add_opnd(r);
+  for (auto& l : b.join_lkey) add_opnd(l);
+  const int nfact = (int)opnds.size();
+  std::vector<std::vector<int>> pay(nref + 1);
+  for (auto& r : refs_used) {
+    if (r.obj == 0) continue;
+    if (r.obj > nref || join_of_obj[r.obj] < 0)
+      return x->fail(SVM_E_INVALID_ARG, "Map references object " + std::to_string(r.obj) + " that is not joined");
+    const ObjectPtr& o = refs[r.obj - 1];
+    if (r.col < 0 || r.col >= o->ncols) return x->fail(SVM_E_INVALID_ARG, "column out of range");
+    if (o->types[r.col] != SVM_INT32) return x->fail(SVM_E_UNSUPPORTED, "joined columns in a Map must be Int32");
+    auto& v = pay[r.obj];
+    if (std::find(v.begin(), v.end(), r.col) == v.end()) v.push_back(r.col);
+  }
+  for (int k = 1; k <= nref; k++) std::sort(pay[k].begin(), pay[k].end());
+  for (int k = 1; k <= nref; k++)
+    for (int c : pay[k]) add_opnd(ColRef{k, c});
   if (b.select_exp.size() > 16) return x->fail(SVM_E_UNSUPPORTED, "more than 16 projected columns");
   if (opnds.size() > 16) return x->fail(SVM_E_UNSUPPORTED, "more than 16 input columns referenced");
-  for (auto& r : opnds) {
-    if (r.obj != 0) return x->fail(SVM_E_INVALID_ARG, "Map/Filter references object " + std::to_string(r.obj) +
-                                                          " but the pipeline joins nothing");
+  for (int i = 0; i < nfact; i++) {
+    const ColRef& r = opnds[i];
     if (r.col < 0 || r.col >= src->ncols) return x->fail(SVM_E_INVALID_ARG, "column out of range");
     // String columns are their int32 codes here: StrCmp tests were rewritten
     // onto them, and a bare projection copies them.
@@ -210,10 +262,31 @@ svm_status run_select(Ctx* x, const Bound& b, const ObjectPtr& src) {
     }
   }
   SelectParams sp{};
-  sp.ncols_in = (int)opnds.size();
-  for (size_t k = 0; k < opnds.size(); k++) sp.cols[k] = (const int32_t*)src->col(opnds[k].col);
+  sp.ncols_in = nfact;
+  sp.nopnd = (int)opnds.size();
+  for (int k = 0; k < nfact; k++) sp.cols[k] = (const int32_t*)src->col(opnds[k].col);
   sp.nrows = (long long)src->nrows;
   sp.error = x->d_error;
+  // ---- joined tables, probed in the order the joins are listed
+  std::vector<DimTablePtr> tables;
+  for (size_t j = 0; j < b.join_rkey.size(); j++) {
+    const int k = b.join_rkey[j].obj;
+    DimTablePtr T;
+    svm_status st = build_dim(x, refs[k - 1], b.join_rkey[j].col, pay[k], &T);
+    if (st) return st;
+    tables.push_back(T);
+    sp.dims[j] = T->desc;
+    sp.dims[j].smem_word_off = -1;
+    for (int i = 0; i < nfact; i++)
+      if (opnds[i].obj == 0 && opnds[i].col == b.join_lkey[j].col) sp.join_opnd[j] = i;
+  }
+  sp.ndims = (int)tables.size();
+  for (int i = nfact; i < sp.nopnd; i++) {
+    const ColRef& r = opnds[i];
+    const int d = join_of_obj[r.obj];
+    const auto& pv = pay[r.obj];
+    sp.dop[i - nfact] = Operand{(int8_t)d, (int8_t)(std::find(pv.begin(), pv.end(), r.col) - pv.begin())};
+  }
   if (has_pred) {
     std::vector<int> conj;
     flatten_and(pred, pred.root, &conj);
@@ -874,26 +947,26 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   if (e) return x->cuda_fail(e, "cudaMemsetAsync");
   if (empty) P.row_end = P.row_begin;  // a contradictory filter: no row can pass
 
-  // Launch configuration: ring depth x whether the small dimension tables are
-  // staged in shared memory.  The rule: the most resident blocks per SM, then
-  // the deepest ring, tables staged.  With autotuning, every fitting
-  // candidate is timed once per plan shape on the query itself (each trial
-  // starts from zeroed slots, so the result is the same whichever wins).
-  // With tuning, also the order of two adjacent probes of tables kept in L2
-  // (filters commute; their relative cost depends on the tables' sizes).
-  struct Cand {
-    int nst;
-    bool staged;
-    int swap;  // >= 0: steps swap and swap + 1 exchanged
-    int blocks;
-  };
+  // Launch configuration: the kernel (compiled for the plan's shape with 4
+  // or 8 rows per consumer lane, or the interpreted kernel), ring depth and
+  // whether the small dimension tables are staged in shared memory.  The
+  // rule: a compiled kernel with 4 rows per lane when the shape has one, then
+  // the most resident blocks per SM, the deepest ring, tables staged.  With
+  // autotuning, every fitting candidate is timed once per plan shape on the
+  // query itself (each trial starts from zeroed slots, so the result is the
+  // same whichever wins), and also the order of two adjacent probes of
+  // tables kept in L2 (filters commute; their relative cost depends on the
+  // tables' sizes).
+  using Cand = Ctx::StarLaunch;
   std::vector<int> staged_off(P.ndims);
   for (int d = 0; d < P.ndims; d++) staged_off[d] = P.dims[d].smem_word_off;
   const int staged_words = P.smem_table_words;
   bool any_staged = false;
   for (int d = 0; d < P.ndims; d++) any_staged |= staged_off[d] >= 0;
   const std::vector<Step> steps0(P.steps, P.steps + P.nsteps);
-  const std::string shape = x->cfg.autotune ? star_shape_key(P) : std::string();  // as planned
+  const std::string shape = x->cfg.autotune ? star_shape_key(P) + "|pin" + std::to_string(x->pin_rows) + "," +
+                                                 std::to_string(x->pin_stages) + "," + std::to_string(x->pin_staged)
+                                           : std::string();  // as planned
   auto configure = [&](const Cand& c) {
     P.nstages = c.nst;
     for (int d = 0; d < P.ndims; d++) P.dims[d].smem_word_off = c.staged ? staged_off[d] : -1;
@@ -902,6 +975,14 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
     if (c.swap >= 0) std::swap(P.steps[c.swap], P.steps[c.swap + 1]);
     flatten_plan(P);
   };
+  auto smem_of = [&](const Cand& c) { return c.rows ? star_plan_smem_bytes(P, c.rows) : star_smem_bytes(P); };
+  auto grid_of = [&](const Cand& c, size_t sm) {
+    return c.rows ? star_plan_grid_size(P, c.rows, sm) : star_grid_size(P, sm);
+  };
+  auto launch = [&](const Cand& c, size_t sm) {
+    return c.rows ? launch_star_plan(P, c.rows, grid_of(c, sm), sm, x->stream)
+                  : launch_star(P, grid_of(c, sm), star_block_size(), sm, x->stream);
+  };
   std::vector<int> swaps = {-1};
   if (x->cfg.autotune)
     for (int k = 0; k + 1 < P.nsteps; k++) {
@@ -909,37 +990,61 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
       if (a.kind == STEP_PROBE && z.kind == STEP_PROBE && staged_off[a.dim] < 0 && staged_off[z.dim] < 0)
         swaps.push_back(k);
     }
-  std::vector<Cand> cands;
+  struct Fit {
+    Cand c;
+    int blocks;
+  };
+  std::vector<Fit> cands;
   for (int sw : swaps)
     for (int staged = 1; staged >= (any_staged ? 0 : 1); staged--)
-      for (int nst = kStages; nst >= 2; nst--) {
-        Cand c{nst, staged != 0, sw, 0};
-        configure(c);
-        const size_t sm = star_smem_bytes(P);
-        c.blocks = sm <= 200 * 1024 ? star_blocks_per_sm(P, sm) : 0;
-        if (c.blocks > 0) cands.push_back(c);
-      }
-  if (cands.empty()) return x->fail(SVM_E_UNSUPPORTED, "shared-memory plan too large");
-  Cand pick = cands[0];
-  for (const Cand& c : cands)
-    if (c.swap < 0 && c.staged && (c.blocks > pick.blocks || !pick.staged)) pick = c;
+      for (int rows : {4, 8, 0})
+        for (int nst = kStages; nst >= 2; nst--) {
+          if ((x->pin_rows >= 0 && rows != x->pin_rows) || (x->pin_stages && nst != x->pin_stages) ||
+              (x->pin_staged >= 0 && staged != x->pin_staged))
+            continue;
+          Cand c;
+          c.nst = nst;
+          c.staged = staged != 0;
+          c.swap = sw;
+          c.rows = rows;
+          configure(c);
+          if (rows && !star_plan_available(P, rows)) continue;
+          const size_t sm = smem_of(c);
+          if (sm > 200 * 1024) continue;
+          const int blocks = rows ? star_plan_blocks_per_sm(P, rows, sm) : star_blocks_per_sm(P, sm);
+          if (blocks > 0) cands.push_back({c, blocks});
+        }
+  if (cands.empty())
+    return x->fail(SVM_E_UNSUPPORTED, x->pin_rows >= 0 || x->pin_stages || x->pin_staged >= 0
+                                          ? "no launch configuration of this plan fits the pinned choices"
+                                          : "shared-memory plan too large");
+  auto rule_rank = [](const Fit& f) {  // larger is preferred
+    return (f.c.rows == 4 ? 2 : f.c.rows == 8 ? 1 : 0) * 1000000 + f.blocks * 1000 + f.c.nst * 10 + (f.c.staged ? 1 : 0);
+  };
+  Cand pick = cands[0].c;
+  int best_rank = -1;
+  for (const Fit& f : cands)
+    if (f.c.swap < 0 && rule_rank(f) > best_rank) {
+      best_rank = rule_rank(f);
+      pick = f.c;
+    }
   cudaEvent_t ev;
   if (x->cfg.autotune && cands.size() > 1) {
     const std::string& key = shape;
     auto hit = x->star_tune.find(key);
     if (hit != x->star_tune.end()) {
-      pick = Cand{std::get<0>(hit->second), std::get<1>(hit->second), std::get<2>(hit->second), 1};
+      pick = hit->second;
     } else {
       cudaEvent_t t0, t1;
       cudaEventCreate(&t0);
       cudaEventCreate(&t1);
       float best = 0.f;
-      for (const Cand& c : cands) {
-        configure(c);
-        const size_t sm = star_smem_bytes(P);
+      for (const Fit& f : cands) {
+        configure(f.c);
+        const size_t sm = smem_of(f.c);
         if (!e) e = cudaMemsetAsync(sums, 0, agg_bytes, x->stream);
         if (!e) e = cudaEventRecord(t0, x->stream);
-        if (!e) e = launch_star(P, star_grid_size(P, sm), star_block_size(), sm, x->stream);
+        if (!e) e = launch(f.c, sm);
         if (!e) e = cudaEventRecord(t1, x->stream);
         if (!e) e = cudaEventSynchronize(t1);
         float ms = 0.f;
@@ -947,21 +1052,38 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
         if (e) break;
         if (best == 0.f || ms < best) {
           best = ms;
-          pick = c;
+          pick = f.c;
         }
       }
       cudaEventDestroy(t0);
       cudaEventDestroy(t1);
       if (e) return x->cuda_fail(e, "star kernel tuning");
-      x->star_tune[key] = std::make_tuple(pick.nst, pick.staged, pick.swap);
+      x->star_tune[key] = pick;
       if ((e = cudaMemsetAsync(sums, 0, agg_bytes, x->stream))) return x->cuda_fail(e, "cudaMemsetAsync");
     }
   }
   configure(pick);
-  size_t smem = star_smem_bytes(P);
-  int grid = star_grid_size(P, smem);
+  size_t smem = smem_of(pick);
+  int grid = grid_of(pick, smem);
+  {
+    std::string steps;
+    for (int k = 0; k < P.nsteps; k++) {
+      const Step& st = P.steps[k];
+      steps += (k ? "," : "") + std::string(st.kind == STEP_RANGE ? "range" : st.layout == LAYOUT_HASH ? "hash"
+                                                                     : st.smem_word_off >= 0 ? "smem"
+                                                                                             : "l2");
+      if (st.kind == STEP_PROBE && st.layout == LAYOUT_DENSE) steps += std::to_string(st.entry_bits);
+    }
+    x->last_launch = std::string("{\"kernel\": \"") + (pick.rows ? "compiled plan" : "interpreted") +
+                     "\", \"rows_per_lane\": " + std::to_string(pick.rows ? pick.rows : 4) +
+                     ", \"ring_stages\": " + std::to_string(pick.nst) + ", \"tables_staged\": " +
+                     (pick.staged ? "true" : "false") + ", \"steps\": \"" + steps + "\", \"grid\": " +
+                     std::to_string(grid) + ", \"block\": " + std::to_string(star_block_size()) +
+                     ", \"smem_bytes\": " + std::to_string(smem) + ", \"tuned\": " +
+                     (x->cfg.autotune && cands.size() > 1 ? "true" : "false") + "}";
+  }
   x->prof_begin(SVM_K_STAR, &ev);
-  e = launch_star(P, grid, star_block_size(), smem, x->stream);
+  e = launch(pick, smem);
   x->prof_end(SVM_K_STAR, ev);
   if (e) return x->cuda_fail(e, "star kernel");
 
@@ -1802,7 +1924,7 @@ svm_status run_pipeline(Ctx* x, const svm_pipeline* p) {
   std::vector<ObjectPtr> refs;
   svm_status st = resolve(x, p, &b, &src, &refs);
   if (st) return st;
-  if (!b.is_reduce) return run_select(x, b, src);
+  if (!b.is_reduce) return run_select(x, b, src, refs);
   return run_star(x, b, src, refs);
 }
 

@@ -371,9 +371,17 @@ inline void flatten_plan(StarParams& P) {
 }
 
 // ---------------------------------------------------------------- select (Map) pipelines
+// Operands 0..ncols_in-1 are source columns; with joins, operands
+// ncols_in..nopnd-1 are payload fields of the joined tables (dop[k]: table
+// and field), read once every join of the row has matched.
 struct SelectParams {
   const int32_t* cols[16];
   int ncols_in;
+  int nopnd;                        // ncols_in + joined payload operands
+  Operand dop[16];                  // operand ncols_in + k: {table, payload field}
+  int ndims;                        // joins, probed in order after the conjuncts
+  DimDesc dims[kMaxDims];
+  int join_opnd[kMaxDims];          // operand holding join d's key (a source column)
   long long nrows;
   int npred;                        // conjunct programs over input columns (operand = column)
   Prog pred[4];

@@ -230,6 +230,18 @@ class Engine:
         return keys, mets
 
     # ------------------------------------------------------------ profiling
+    def pin_launch(self, rows_per_lane: int = -1, ring_stages: int = 0, tables_staged: int = -1):
+        """Narrows the fused scan's launch configurations (svm_pin_launch);
+        the defaults lift every pin."""
+        self._check(self.lib.svm_pin_launch(self.h, rows_per_lane, ring_stages, tables_staged))
+
+    def last_launch(self) -> dict:
+        """The last fused scan's launch configuration (svm_last_launch)."""
+        import json
+        buf = ctypes.create_string_buffer(1024)
+        self._check(self.lib.svm_last_launch(self.h, buf, len(buf)))
+        return json.loads(buf.value.decode()) if buf.value else {}
+
     def test_device_wait(self, wait_polls: int = 0, stall_copies: bool = False):
         """Test hook: the fused scan's mbarrier poll limit (0 = default) and
         whether its copy warp issues no copies (svm_test_device_wait)."""

@@ -95,6 +95,24 @@ def fact_pipeline(pid: str, source: str, src_schema: ObjectInfo, dims: list[str]
     return t.pipe_info
 
 
+def join_map_pipeline(pid: str, source: str, src_schema: ObjectInfo, dims: list[str],
+                      joins: list[tuple[str, str]], select: str, predication: str | None = None) -> PipelineInfo:
+    """Joined projection: Source -> [Filter] -> JoinWith... -> Map -> Sink, no
+    ReduceBy (the reference generates its join block, then its select block,
+    codegen/codegen.cpp:121-180).  Sink: one int32 column per expression."""
+    n = len(str_split(select, ","))
+    out = create_schema([I32] * n, [4] * n)
+    t = PipelineTest(pid).add_pre(source, *dims)
+    t.add_operator(OpType.Source, {"type": "object"}, src_schema)
+    if predication:
+        t.add_operator(OpType.Filter, {"predication": predication}, out)
+    for lk, rk in joins:
+        t.add_operator(OpType.JoinWith, {"lkey": lk, "rkey": rk}, out)
+    t.add_operator(OpType.Map, {"select": select}, out)
+    t.add_operator(OpType.Sink, {}, out)
+    return t.pipe_info
+
+
 # ------------------------------------------------------------------ Java DSL mirror
 @dataclass
 class Table:

@@ -24,7 +24,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import datagen as dg
-from .pipeline import dim_pipeline, fact_pipeline
+from .pipeline import dim_pipeline, fact_pipeline, join_map_pipeline
 from .proto import ObjectInfo, PipelineInfo, ValType, create_schema
 
 FACT_COLS = {
@@ -34,6 +34,7 @@ FACT_COLS = {
         "supplycost"],
 }
 FACT_COLS[5] = FACT_COLS[2]
+FACT_COLS[7] = FACT_COLS[2]
 
 # String widths of config 5's geography columns (bytes, NUL-padded).
 CITY_W, NATION_W, REGION_W = 10, 15, 12
@@ -112,7 +113,7 @@ class Workload:
 
     def fact_bytes_per_row(self) -> int:
         """Algorithmic bytes: 4 per distinct fact column the query reads."""
-        return 4 * {0: 4, 1: 3, 2: 5, 5: 5}[self.config]
+        return 4 * {0: 4, 1: 3, 2: 5, 5: 5, 7: 6}[self.config]
 
     def dim_schema(self, name: str) -> ObjectInfo:
         return schema_of(self.dims[name])
@@ -199,6 +200,18 @@ def make(config: int, *, fact_rows: int | None = None, seed: int = dg.DEFAULT_SE
                                 [("$(0.0)", "$(1.0)"), ("$(0.5)", "$(2.0)"), ("$(0.6)", "$(3.0)")],
                                 "$(2.1),$(3.1),$(1.1)", "$(0.7)-$(0.8)")
         w.key_num = 3
+    elif config == 7:
+        # Joined projection (no ReduceBy) over the four-dimension schema: the
+        # rows of a discount band whose date, customer and supplier keys all
+        # match, with columns from the fact table and every joined object.
+        w = make(2, fact_rows=dflt(fact_rows, 6_000_000), seed=seed, tuple_per_bulk=tuple_per_bulk,
+                 n_part=n_part, n_cust=n_cust, n_supp=n_supp, qseed=qs)
+        w.config = 7
+        w.query = join_map_pipeline("q7", "lineorder", w.fact_schema(), ["q2_date", "q2_cust", "q2_supp"],
+                                    [("$(0.0)", "$(1.0)"), ("$(0.5)", "$(2.0)"), ("$(0.6)", "$(3.0)")],
+                                    "$(0.0),$(1.1),$(2.1),$(3.1),$(0.7)-$(0.8),$(0.5)",
+                                    predication="$(0.2)<=4")
+        w.key_num = -1  # no ReduceBy: the result is rows (read_all)
     else:
         raise ValueError(f"no config {config}")
     return w

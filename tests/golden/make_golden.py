@@ -7,7 +7,9 @@ For every case below it runs the workload through the reference's OWN
 CodeGen and runtime headers (oracle mode "ref", built by oracle/build_ref.sh
 from the reference sources) and records the merged, key-sorted result.  For
 the code generator it records the SHA-256 of the host code the reference's
-CodeGen emits for each pipeline (the text itself is not stored).  A GPU host
+CodeGen emits for each pipeline (the text itself is not stored).  Joined
+projections (JoinWith -> Map, no ReduceBy) go to reference_joinmap.json with
+their output rows in order.  A GPU host
 without the reference tree runs the tests against these files instead.
 """
 from __future__ import annotations
@@ -52,6 +54,19 @@ CASES = [
 ]
 
 
+# Joined projections (JoinWith -> Map, no ReduceBy): the rows themselves.
+JOIN_MAP_CASES = [
+    ("c7_small", 7, dict(fact_rows=200_000, tuple_per_bulk=100_000, n_part=20_000, n_cust=60_000,
+                         n_supp=8_000), False),
+    # unfiltered 300 K customers in a 1.5 M-slot table: rows whose customer key was dropped vanish
+    ("c7_drops", 7, dict(fact_rows=60_000, tuple_per_bulk=300_000, n_part=20_000, n_cust=300_000,
+                         n_supp=8_000, qseed=7), True),
+    # joined objects larger than one bulk: only their bulk 0 is joinable; several fact bulks
+    ("c7_bulk0", 7, dict(fact_rows=150_000, tuple_per_bulk=40_000, n_part=20_000, n_cust=100_000,
+                         n_supp=8_000, qseed=7), False),
+]
+
+
 def build_case(cfg, kw, unfiltered_cust):
     w = W.make(cfg, **kw)
     if unfiltered_cust:
@@ -80,6 +95,22 @@ def main():
         print(name, len(keys), "equals_exact" if same else "differs from exact")
     with open(os.path.join(HERE, "reference_results.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
+    rows = {}
+    for name, cfg, kw, unf in JOIN_MAP_CASES:
+        w = build_case(cfg, kw, unf)
+        cols = oracle.run_workload_rows(w, "ref", threads=8)
+        exact = oracle.exact_workload_rows(w)
+        same = all(len(a) == len(b) and (a == b).all() for a, b in zip(cols, exact))
+        texts = {}
+        for p in w.dim_pipelines + [w.query]:
+            refs = [dim_schema(w, i) for i in p.pre_pipeline_id[1:]] if p is w.query else []
+            texts[p.id] = hashlib.sha256(oracle.ref_codegen(p, refs).encode()).hexdigest()
+        rows[name] = {"config": cfg, "kwargs": kw, "unfiltered_customer": unf, "params": w.params,
+                      "columns": [c.tolist() for c in cols], "equals_exact": bool(same),
+                      "codegen_sha256": texts}
+        print(name, len(cols[0]), "equals_exact" if same else "differs from exact")
+    with open(os.path.join(HERE, "reference_joinmap.json"), "w") as f:
+        json.dump(rows, f, sort_keys=True)
 
 
 def dim_schema(w, pid):

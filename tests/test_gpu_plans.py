@@ -1,0 +1,83 @@
+"""The fused scan's launch variants all compute the reference's result.
+
+Each golden case (the reference's own results for configs 0, 1, 2 and 5 at
+test scale, including a dimension the capped insert drops keys from) runs
+under every pinned choice the tuner varies: the kernel compiled for the
+plan's shape with 4 or 8 rows per consumer lane, or the interpreted kernel;
+2 or 3 ring stages; small tables staged in shared memory or probed in L2.
+Every variant must equal the golden rows bit for bit, and the shapes of
+configs 0, 1 and 2 must have a compiled kernel (the launch reports it)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from shadowvm_gb300 import SvmError
+from shadowvm_gb300 import workloads as W
+from shadowvm_gb300.pipeline import dim_pipeline
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_results.json")))
+CASES = ["c0_small", "c0_q2", "c1_small", "c1_q3", "c2_small", "c2_q11", "c2_drops", "c2_bulk0", "c5_small"]
+
+
+def golden_rows(case, key_num):
+    rows = len(case["sums"])
+    keys = np.array(case["keys"], np.int32).reshape(rows, key_num)
+    sums = np.array(case["sums"], np.int64).reshape(rows, -1) if rows else np.zeros((0, 1), np.int64)
+    return keys, sums
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_every_launch_variant_equals_the_reference(engine_factory, name):
+    case = GOLDEN[name]
+    w = W.make(case["config"], **case["kwargs"])
+    if case["unfiltered_customer"]:
+        w.dim_pipelines[1] = dim_pipeline("q2_cust", "customer", W.int_schema(4), "$(0.0),$(0.2)", None)
+    gk, gs = golden_rows(case, w.key_num)
+    eng = engine_factory(tuple_per_bulk=w.tuple_per_bulk, autotune=False)
+    W.load_engine(eng, w)
+    for p in w.dim_pipelines:
+        eng.run(p)
+    kernels = set()
+    for rows in (4, 8, 0):
+        for stages in (2, 3):
+            for staged in (1, 0):
+                eng.pin_launch(rows, stages, staged)
+                try:
+                    eng.run(w.query)
+                except SvmError as e:
+                    assert rows != 0, e  # the interpreted kernel takes every plan
+                    continue
+                got = eng.result(w.query.id, w.key_num)
+                launch = eng.last_launch()
+                assert launch["ring_stages"] == stages
+                kernels.add((launch["kernel"], launch["rows_per_lane"]))
+                np.testing.assert_array_equal(got[0], gk, err_msg=f"{rows} rows, {stages} stages, staged {staged}")
+                np.testing.assert_array_equal(got[1], gs, err_msg=f"{rows} rows, {stages} stages, staged {staged}")
+    eng.pin_launch()
+    if case["config"] in (0, 1, 2) and not case["unfiltered_customer"]:
+        assert ("compiled plan", 4) in kernels and ("compiled plan", 8) in kernels, kernels
+    assert ("interpreted", 4) in kernels
+
+
+def test_tuned_launch_equals_the_fixed_rule(engine_factory):
+    """The tuner's pick (timed on first use of the shape, cached after) and the
+    rule's pick give the same rows; the tuned pick is reported."""
+    case = GOLDEN["c2_small"]
+    w = W.make(case["config"], **case["kwargs"])
+    gk, gs = golden_rows(case, w.key_num)
+    for tune in (True, False):
+        eng = engine_factory(tuple_per_bulk=w.tuple_per_bulk, autotune=tune)
+        W.load_engine(eng, w)
+        for _ in range(2):
+            k, s = W.run_engine(eng, w)
+            np.testing.assert_array_equal(k, gk)
+            np.testing.assert_array_equal(s, gs)
+        launch = eng.last_launch()
+        assert launch["tuned"] == tune
+        if not tune:
+            assert launch["kernel"] == "compiled plan" and launch["rows_per_lane"] == 4
+        eng.close()

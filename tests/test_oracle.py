@@ -110,3 +110,40 @@ def test_exact_evaluator_c_semantics():
     np.testing.assert_array_equal(S.evaluate(S.parse("$(0.0)*$(0.1)"), env, 3), [-14, -14, -2])
     np.testing.assert_array_equal(S.evaluate(S.parse("$(0.0)>0 && $(0.1)>0 || !$(0.0)"), env, 3), [0, 0, 1])
     np.testing.assert_array_equal(S.evaluate(S.parse("010 + 0x10"), env, 3), [24, 24, 24])
+
+
+JOINMAP = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_joinmap.json")))
+
+
+@pytest.mark.parametrize("name", sorted(JOINMAP))
+def test_port_reproduces_reference_joined_projections(name):
+    case = JOINMAP[name]
+    w = build_case(case)
+    assert w.params == case["params"]
+    cols = oracle.run_workload_rows(w, "port", threads=4)
+    assert len(cols) == len(case["columns"])
+    for got, want in zip(cols, case["columns"]):
+        np.testing.assert_array_equal(got, np.array(want, np.int32))
+    exact = oracle.exact_workload_rows(w)
+    same = all(len(a) == len(b) and (a == b).all() for a, b in zip(exact, cols))
+    assert same == case["equals_exact"]
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference-compiled checker not built (oracle/_ref)")
+@pytest.mark.parametrize("name", sorted(JOINMAP))
+def test_joined_projection_fixtures_equal_the_live_reference(name):
+    case = JOINMAP[name]
+    w = build_case(case)
+    cols = oracle.run_workload_rows(w, "ref", threads=4)
+    for got, want in zip(cols, case["columns"]):
+        np.testing.assert_array_equal(got, np.array(want, np.int32))
+
+
+@pytest.mark.parametrize("name", sorted(JOINMAP))
+def test_joined_projection_codegen_text_matches_reference_codegen(name):
+    case = JOINMAP[name]
+    w = build_case(case)
+    schemas = {p.id: [op.output for op in p.workflow if op.type == 7][0] for p in w.dim_pipelines}
+    for p in w.dim_pipelines + [w.query]:
+        refs = [schemas[i] for i in p.pre_pipeline_id[1:]] if p is w.query else []
+        assert hashlib.sha256(oracle.port_codegen(p, refs).encode()).hexdigest() == case["codegen_sha256"][p.id]
