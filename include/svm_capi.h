@@ -21,6 +21,7 @@
  *                                 ReduceTask (core/pipeline.cu:360-472); result cached by pipeline
  *                                 id like ShadowVMService::cached_obj (service/service.hpp:92)
  *   svm_run_batch                 no counterpart: many RunPipelineCMD calls folded into one launch
+ *   svm_batch_begin/wait/release  no counterpart: the same, enqueued without waiting (folds in flight)
  *   svm_pipeline_footprint        no counterpart: device bytes a pipeline needs (served admission)
  *   svm_object_load_text          Loader::Host (core/operator.cpp:24-48): delimited text -> columns
  *   svm_object_put_columns        RamObject bulks with String columns (ValType String, com/svm.proto:62-72;
@@ -211,6 +212,32 @@ svm_status svm_run_pipeline(svm_ctx* ctx, const svm_pipeline* pipe);
  * Every output is stored as in svm_run_pipeline.  The result of each pipeline
  * equals its result from svm_run_pipeline. */
 svm_status svm_run_batch(svm_ctx* ctx, int n, const svm_pipeline* pipes);
+
+/* Folds in flight (no counterpart in the reference, whose service runs one
+ * synchronous RPC at a time, service/service.cu:25-63).  svm_batch_begin
+ * plans `n` pipelines like svm_run_batch and enqueues their device work
+ * without waiting for it: reduce pipelines over one fact table go into
+ * batched launches whose result store holds every group the queries can
+ * produce, so no host step is needed between the launches and the results.
+ * Map pipelines, reduce pipelines the batch kernel does not take, and ones
+ * the cost model runs alone complete inside the call.  With host_results
+ * != 0 every result is also copied, behind the fold's work, into page-locked
+ * staging.  While a fold's work runs, the caller may plan and begin the next
+ * fold (the device runs them in order on the context's stream).
+ * svm_batch_wait blocks until the fold's device work is done (without
+ * holding the context, so other calls proceed meanwhile), stores every
+ * result as object `id` as svm_run_batch does, and reports each pipeline's
+ * row count (nrows_out[i], input order) and the bytes of the host copy
+ * (*needed; 0 without host_results).  svm_batch_release copies the staged
+ * results to `host` (when not NULL; svm_objects_read's layout: for each
+ * pipeline in input order, each column's rows from an 8-byte-aligned
+ * offset) and frees the fold; every fold must be released, also one whose
+ * wait failed.  The objects a fold reads must not be replaced until its
+ * wait returns. */
+typedef struct svm_fold svm_fold;
+svm_status svm_batch_begin(svm_ctx* ctx, int n, const svm_pipeline* pipes, int host_results, svm_fold** out);
+svm_status svm_batch_wait(svm_ctx* ctx, svm_fold* fold, unsigned long long* nrows_out, unsigned long long* needed);
+svm_status svm_batch_release(svm_ctx* ctx, svm_fold* fold, void* host, unsigned long long cap);
 
 /* Device bytes that running `pipe` needs beyond what is resident (group
  * slots, finalize scratch and the largest possible result), for admission by

@@ -113,6 +113,9 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "svm_run_pipeline": (I, [P, ctypes.POINTER(svm_pipeline)]),
         "svm_run_batch": (I, [P, I, ctypes.POINTER(svm_pipeline)]),
         "svm_pipeline_footprint": (I, [P, ctypes.POINTER(svm_pipeline), ctypes.POINTER(U64)]),
+        "svm_batch_begin": (I, [P, I, ctypes.POINTER(svm_pipeline), I, ctypes.POINTER(P)]),
+        "svm_batch_wait": (I, [P, P, ctypes.POINTER(U64), ctypes.POINTER(U64)]),
+        "svm_batch_release": (I, [P, P, P, U64]),
         "svm_profile_enable": (I, [P, I]),
         "svm_profile_reset": (I, [P]),
         "svm_profile_read": (I, [P, I, ctypes.POINTER(U64), ctypes.POINTER(D)]),

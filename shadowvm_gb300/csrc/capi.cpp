@@ -124,6 +124,31 @@ svm_status Ctx::upload(void* dst, const void* src, size_t bytes) {
   return SVM_OK;
 }
 
+svm_status Ctx::pinned_take(size_t bytes, PinnedBlock* out) {
+  size_t best = pinned_pool.size();
+  for (size_t i = 0; i < pinned_pool.size(); i++)
+    if (pinned_pool[i].bytes >= bytes && (best == pinned_pool.size() || pinned_pool[i].bytes < pinned_pool[best].bytes))
+      best = i;
+  if (best < pinned_pool.size()) {
+    *out = pinned_pool[best];
+    pinned_pool.erase(pinned_pool.begin() + (long)best);
+    return SVM_OK;
+  }
+  size_t want = 4096;
+  while (want < bytes) want *= 2;
+  void* p = nullptr;
+  cudaError_t e = cudaMallocHost(&p, want);
+  if (e) return cuda_fail(e, "cudaMallocHost");
+  out->p = p;
+  out->bytes = want;
+  return SVM_OK;
+}
+
+void Ctx::pinned_give(PinnedBlock* b) {
+  if (b->p) pinned_pool.push_back(*b);
+  *b = PinnedBlock{};
+}
+
 svm_status Ctx::pinned_reserve(size_t bytes) {
   if (pinned_bytes >= bytes) return SVM_OK;
   if (pinned) cudaFreeHost(pinned);
@@ -291,6 +316,8 @@ void svm_destroy(svm_ctx* c) {
   x->scratch.reset();
   x->trim_pool(0);
   if (x->pinned) cudaFreeHost(x->pinned);
+  for (auto& b : x->pinned_pool) cudaFreeHost(b.p);
+  x->pinned_pool.clear();
   for (int i = 0; i < svm::Ctx::kCopyStreams; i++)
     if (x->copy_stream[i]) cudaStreamDestroy(x->copy_stream[i]);
   for (int i = 0; i <= svm::Ctx::kCopyStreams; i++)
@@ -698,6 +725,49 @@ svm_status svm_run_batch(svm_ctx* c, int n, const svm_pipeline* p) {
   cudaSetDevice(x->device);
   x->err.clear();
   return svm::run_batch(x, n, p);
+}
+
+struct svm_fold {
+  void* impl = nullptr;
+};
+
+svm_status svm_batch_begin(svm_ctx* c, int n, const svm_pipeline* p, int host_results, svm_fold** out) {
+  if (!c || (n > 0 && !p) || n < 0 || !out) return SVM_E_INVALID_ARG;
+  *out = nullptr;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  cudaSetDevice(x->device);
+  x->err.clear();
+  void* f = nullptr;
+  svm_status st = svm::batch_begin(x, n, p, host_results, &f);
+  if (st) return st;
+  *out = new svm_fold{f};
+  return SVM_OK;
+}
+
+svm_status svm_batch_wait(svm_ctx* c, svm_fold* fold, unsigned long long* nrows_out, unsigned long long* needed) {
+  if (!c || !fold || !fold->impl) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  // The wait for the fold's device work holds no lock, so that the next fold
+  // can be planned and enqueued meanwhile.
+  cudaSetDevice(x->device);
+  svm::fold_sync(fold->impl);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  x->err.clear();
+  return svm::batch_wait(x, fold->impl, nullptr, 0, nrows_out, needed);
+}
+
+svm_status svm_batch_release(svm_ctx* c, svm_fold* fold, void* host, unsigned long long cap) {
+  if (!c || !fold) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  cudaSetDevice(x->device);
+  x->err.clear();
+  svm_status st = SVM_OK;
+  if (host && fold->impl) st = svm::batch_wait(x, fold->impl, host, cap, nullptr, nullptr);
+  svm::batch_discard(x, fold->impl);
+  delete fold;
+  return st;
 }
 
 svm_status svm_pipeline_footprint(svm_ctx* c, const svm_pipeline* p, unsigned long long* bytes) {

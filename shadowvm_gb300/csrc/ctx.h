@@ -108,6 +108,12 @@ struct MergedTable {
   unsigned long long stamp = 0;
 };
 
+// A page-locked host block from the context's pool (see Ctx::pinned_take).
+struct PinnedBlock {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
 struct ProfEvent {
   int cls;
   cudaEvent_t a, b;
@@ -128,6 +134,11 @@ struct Ctx {
   // Pinned host staging for bulk reads (grows, kept).
   void* pinned = nullptr;
   size_t pinned_bytes = 0;
+  // Page-locked blocks of folds in flight come from this pool and return to
+  // it (cudaFreeHost would synchronise the device); freed at destroy.
+  std::vector<PinnedBlock> pinned_pool;
+  svm_status pinned_take(size_t bytes, PinnedBlock* out);
+  void pinned_give(PinnedBlock* b);
   // Copy streams for large host-to-device uploads (created on first use).
   static constexpr int kCopyStreams = 4;
   cudaStream_t copy_stream[kCopyStreams] = {};
@@ -235,6 +246,15 @@ inline svm_status device_error_status(int code, const char** msg) {
 svm_status noalloc_prepare(Ctx* x);
 
 // Pipelines (pipeline.cpp).
+// Folds: batch_begin enqueues a batch and returns an opaque fold without
+// waiting for its device work; batch_wait completes it (results stored as
+// objects, optionally copied to `host` in svm_objects_read's layout) and
+// frees it; batch_discard frees a fold that will not be waited for.
+svm_status batch_begin(Ctx* x, int n, const svm_pipeline* p, int want_host, void** fold);
+svm_status batch_wait(Ctx* x, void* fold, void* host, unsigned long long cap, unsigned long long* nrows_out,
+                      unsigned long long* needed);
+void batch_discard(Ctx* x, void* fold);
+void fold_sync(void* fold);  // waits for the fold's device work (no context state touched)
 svm_status run_pipeline(Ctx* ctx, const svm_pipeline* p);
 svm_status run_batch(Ctx* ctx, int n, const svm_pipeline* p);
 svm_status pipeline_footprint(Ctx* ctx, const svm_pipeline* p, unsigned long long* bytes);

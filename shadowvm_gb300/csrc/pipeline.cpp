@@ -1531,7 +1531,69 @@ svm_status merged_table(Ctx* x, MergePlan* mp, int g, unsigned int* conflict, st
 // One batched launch over queries that share a fact table: queries whose
 // probes all hit merged tables run in the merged kernel, the others in the
 // per-query batch kernel; one finalize covers both.
-svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
+// A batch enqueued without waiting (svm_batch_begin): its device buffers,
+// the result store sized for every group the queries can produce, and the
+// slots in the fold's pinned host buffer where its result bounds and error
+// word arrive.  Completed by finish_part once the fold's event has fired.
+struct FoldPart {
+  std::vector<BatchItem> items;
+  std::vector<int> order;            // launch order -> items index
+  DevBufPtr dev;                     // descriptors, slots, finalize scratch, bounds, error word
+  ObjectPtr store;                   // 3 int32 key columns + 3 int64 sum columns
+  size_t host_off = 0;               // first uint64 of this part in the fold's pinned buffer
+  int nq = 0;
+};
+
+// A fold in flight: every pipeline of an svm_batch_begin call, in input
+// order.  A reduce pipeline batched into part `part` at launch position
+// `pos` is completed when the fold's event fires; every other pipeline (a
+// Map, one the batch kernel does not take, one run alone by the cost model)
+// ran to completion inside svm_batch_begin.  With host results requested,
+// each part's whole result store and each completed pipeline's columns are
+// copied behind the fold's work into pinned staging.
+struct Fold {
+  struct Res {
+    std::string id;
+    int part = -1, pos = -1;
+    ObjectPtr done;                  // completed inside begin
+    size_t stage_off = 0;            // completed: its columns' first byte in staging
+  };
+  std::vector<Res> res;
+  std::vector<FoldPart> parts;
+  std::vector<size_t> part_stage;    // per part: first byte of its store copy in staging
+  std::vector<unsigned long long> part_groups;  // per part: store rows
+  bool want_host = false;
+  PinnedBlock bounds, stage;         // pinned: per part nq + 2 words; the result copies
+  cudaEvent_t done = nullptr;
+};
+
+// Each batched query's result object: a view of its rows [hb[j], hb[j + 1])
+// in the batch's result store (j its launch position).
+svm_status store_batch_results(Ctx* x, const std::vector<BatchItem>& items, const std::vector<int>& order,
+                               const ObjectPtr& all, const unsigned long long* hb) {
+  for (size_t j = 0; j < order.size(); j++) {
+    const BatchItem& it = items[order[j]];
+    auto out = std::make_shared<Object>();
+    out->id = it.id;
+    out->version = x->next_version++;
+    out->ncols = it.plan.nkeys + it.plan.nmet;
+    out->types = it.plan.out_types;
+    for (int k = 0; k < it.plan.nkeys; k++) out->storage.push_back(all->storage[k]);
+    for (int m = 0; m < it.plan.nmet; m++) out->storage.push_back(all->storage[kMaxKeys + m]);
+    out->row0 = hb[j];
+    out->nrows = hb[j + 1] - out->row0;
+    out->has_bulks = true;
+    out->bulk0_rows = out->nrows;
+    out->source_rows = out->nrows;
+    svm_status st = translate_keys(x, it.b, out);
+    if (st) return st;
+    x->objects[it.id] = out;
+  }
+  return SVM_OK;
+}
+
+svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items, FoldPart* async_part = nullptr,
+                      unsigned long long* host_bounds = nullptr) {
   const int nq = (int)items.size();
   // Union of the fact columns, identified by their storage.
   std::vector<const void*> ucols;
@@ -1769,7 +1831,6 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
       dmq[j] = mqs[order[j]];
     }
   }
-  x->scratch_reset();
   const size_t qbytes = sizeof(BatchQuery) * nq, mbytes = sizeof(MQuery) * nmerged;
   const size_t fin_words = (total_groups + 1) / 2 + 1 + total_groups + 1 + scan_tmp_words(total_groups);
   // Merged launches: as many queries per launch as their descriptors fit.
@@ -1781,14 +1842,37 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
     }
   const int per_launch = nmerged ? (int)((kMergedSmem - merged_fixed(mst)) / kPerQuery) : 1;
   const int nlaunch = nmerged ? (nmerged + per_launch - 1) / per_launch : 0;
-  const size_t need = qbytes + mbytes + 8 * slot_words + 8 * (nlaunch + 1) + 8 * fin_words + 8 * (nq + 1) + 8 * 1024;
-  if ((st = x->scratch_reserve(need))) return st;
+  const size_t need = qbytes + mbytes + 8 * slot_words + 8 * (nlaunch + 1) + 8 * fin_words + 8 * (nq + 2) + 8 * 1024;
   void *dq, *dm = nullptr, *slots, *ctr, *fin, *bounds;
-  if ((st = x->scratch_take(qbytes, &dq)) || (nmerged && (st = x->scratch_take(mbytes, &dm))) ||
-      (st = x->scratch_take(8 * slot_words, &slots)) || (st = x->scratch_take(8 * (nlaunch + 1), &ctr)) ||
-      (st = x->scratch_take(8 * fin_words, &fin)) || (st = x->scratch_take(8 * (nq + 1), &bounds)))
-    return st;
+  int* err_word = x->d_error;
+  if (async_part) {
+    // The fold's own device buffer (carved like the scratch arena), so that
+    // folds in flight never share scratch.
+    if ((st = x->alloc(need, &async_part->dev))) return st;
+    char* base = (char*)async_part->dev->p;
+    size_t used = 0;
+    auto take = [&](size_t bytes) {
+      void* p = base + used;
+      used += (bytes + 255) & ~size_t(255);
+      return p;
+    };
+    dq = take(qbytes);
+    if (nmerged) dm = take(mbytes);
+    slots = take(8 * slot_words);
+    ctr = take(8 * (nlaunch + 1));
+    fin = take(8 * fin_words);
+    bounds = take(8 * (nq + 2));
+    err_word = (int*)((unsigned long long*)bounds + nq + 1);
+  } else {
+    x->scratch_reset();
+    if ((st = x->scratch_reserve(need))) return st;
+    if ((st = x->scratch_take(qbytes, &dq)) || (nmerged && (st = x->scratch_take(mbytes, &dm))) ||
+        (st = x->scratch_take(8 * slot_words, &slots)) || (st = x->scratch_take(8 * (nlaunch + 1), &ctr)) ||
+        (st = x->scratch_take(8 * fin_words, &fin)) || (st = x->scratch_take(8 * (nq + 1), &bounds)))
+      return st;
+  }
   cudaError_t e = cudaMemcpyAsync(dq, dqs.data(), qbytes, cudaMemcpyHostToDevice, x->stream);
+  if (!e && async_part) e = cudaMemsetAsync(err_word, 0, 8, x->stream);
   if (!e && nmerged) e = cudaMemcpyAsync(dm, dmq.data(), mbytes, cudaMemcpyHostToDevice, x->stream);
   if (!e) e = cudaMemsetAsync(slots, 0, 8 * slot_words, x->stream);
   if (!e) e = cudaMemsetAsync(ctr, 0, 8 * (nlaunch + 1), x->stream);
@@ -1813,7 +1897,7 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
     B.nqueries = qn;
     B.slots = (unsigned long long*)slots;
     B.tile_counter = (unsigned long long*)ctr + part;
-    B.error = x->d_error;
+    B.error = err_word;
     if (merged) {
       B.nprobe = (int)mp.groups.size();
       for (size_t g = 0; g < mp.groups.size(); g++) B.probe[g] = mp.groups[g];
@@ -1856,9 +1940,31 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
   x->prof_begin(SVM_K_FINALIZE, &ev);
   e = launch_batch_finalize(dQ, nq, (unsigned long long*)slots, total_groups, flags, pos, scant, nullptr, x->stream);
   x->prof_end(SVM_K_FINALIZE, ev);
+  if (!e) e = launch_batch_bounds(dQ, nq, pos, total_groups, (unsigned long long*)bounds, x->stream);
+  if (e) return x->cuda_fail(e, "batch finalize");
+  if (async_part) {
+    // No host step: the store holds every group the queries can produce, the
+    // rows are written now, and the bounds and the error word go to the
+    // fold's pinned buffer behind them.
+    std::vector<int> types = {SVM_INT32, SVM_INT32, SVM_INT32, SVM_INT64, SVM_INT64, SVM_INT64};
+    ObjectPtr all = new_result_object(x, "", types, total_groups, &st);
+    if (st) return st;
+    BatchOut o{};
+    for (int k = 0; k < kMaxKeys; k++) o.key[k] = (int32_t*)all->col(k);
+    for (int m = 0; m < kMaxMetrics; m++) o.sum[m] = (long long*)all->col(kMaxKeys + m);
+    x->prof_begin(SVM_K_FINALIZE, &ev);
+    e = launch_batch_finalize(dQ, nq, (unsigned long long*)slots, total_groups, flags, pos, scant, &o, x->stream);
+    x->prof_end(SVM_K_FINALIZE, ev);
+    if (!e) e = cudaMemcpyAsync(host_bounds, bounds, 8 * (nq + 2), cudaMemcpyDeviceToHost, x->stream);
+    if (e) return x->cuda_fail(e, "batch write");
+    async_part->store = all;
+    async_part->order = order;
+    async_part->nq = nq;
+    async_part->items = std::move(items);
+    return SVM_OK;
+  }
   // Only each query's first result row comes back to the host.
   std::vector<unsigned long long> hb(nq + 1);
-  if (!e) e = launch_batch_bounds(dQ, nq, pos, total_groups, (unsigned long long*)bounds, x->stream);
   if (!e) e = cudaMemcpyAsync(hb.data(), bounds, 8 * (nq + 1), cudaMemcpyDeviceToHost, x->stream);
   if (e) return x->cuda_fail(e, "batch finalize");
   if ((st = sync_and_check(x, "batch"))) return st;
@@ -1875,25 +1981,7 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items) {
   x->prof_end(SVM_K_FINALIZE, ev);
   if (e) return x->cuda_fail(e, "batch write");
   if ((st = sync_and_check(x, "batch write"))) return st;
-  for (int j = 0; j < nq; j++) {
-    const BatchQuery& Q = dqs[j];
-    const BatchItem& it = items[order[j]];
-    auto out = std::make_shared<Object>();
-    out->id = it.id;
-    out->version = x->next_version++;
-    out->ncols = Q.nkeys + Q.nmetrics;
-    out->types = it.plan.out_types;
-    for (int k = 0; k < Q.nkeys; k++) out->storage.push_back(all->storage[k]);
-    for (int m = 0; m < Q.nmetrics; m++) out->storage.push_back(all->storage[kMaxKeys + m]);
-    out->row0 = hb[j];
-    out->nrows = hb[j + 1] - out->row0;
-    out->has_bulks = true;
-    out->bulk0_rows = out->nrows;
-    out->source_rows = out->nrows;
-    if ((st = translate_keys(x, it.b, out))) return st;
-    x->objects[it.id] = out;
-  }
-  return SVM_OK;
+  return store_batch_results(x, items, order, all, hb.data());
 }
 
 }  // namespace
@@ -1995,6 +2083,238 @@ svm_status run_batch(Ctx* x, int n, const svm_pipeline* p) {
     }
   }
   return SVM_OK;
+}
+
+
+// ============================================================ folds in flight
+namespace {
+
+// Bytes of a result's host copy in svm_objects_read's layout: every column
+// starts 8-byte aligned.
+unsigned long long host_bytes(const std::vector<int>& types, unsigned long long rows) {
+  unsigned long long b = 0;
+  for (int t : types) b += (rows * (t == SVM_INT64 ? 8 : 4) + 7) & ~7ull;
+  return b;
+}
+
+svm_status fold_fail(Ctx* x, Fold* f, svm_status st) {
+  // Nothing of the fold may still be running when its buffers go back.
+  cudaStreamSynchronize(x->stream);
+  x->pinned_give(&f->bounds);
+  x->pinned_give(&f->stage);
+  if (f->done) cudaEventDestroy(f->done);
+  delete f;
+  return st;
+}
+
+}  // namespace
+
+svm_status batch_begin(Ctx* x, int n, const svm_pipeline* p, int want_host, void** out) {
+  *out = nullptr;
+  auto* F = new Fold;
+  F->want_host = want_host != 0;
+  F->res.resize(n);
+  std::vector<Bound> bounds(n);
+  std::vector<char> reduce(n);
+  std::set<std::string> reduce_ids;
+  svm_status st;
+  for (int i = 0; i < n; i++) {
+    if ((st = bind(x, &p[i], &bounds[i]))) return fold_fail(x, F, st);
+    F->res[i].id = bounds[i].id;
+    reduce[i] = bounds[i].is_reduce;
+    if (reduce[i]) reduce_ids.insert(bounds[i].id);
+  }
+  if ((st = x->pinned_take(8 * (3 * (size_t)n + 2), &F->bounds))) return fold_fail(x, F, st);
+  auto complete_now = [&](int i) -> svm_status {
+    svm_status r = run_pipeline(x, &p[i]);
+    if (!r) F->res[i].done = x->find(F->res[i].id);
+    return r;
+  };
+  bool dependent = false;  // a pipeline reads another's reduce output: everything in order, now
+  for (int i = 0; i < n && !dependent; i++)
+    for (int j = 0; j < p[i].npre; j++)
+      if (p[i].pre_pipeline_id && p[i].pre_pipeline_id[j] && reduce_ids.count(p[i].pre_pipeline_id[j]))
+        dependent = true;
+  if (dependent) {
+    for (int i = 0; i < n; i++)
+      if ((st = complete_now(i))) return fold_fail(x, F, st);
+  } else {
+    for (int i = 0; i < n; i++)
+      if (!reduce[i] && (st = complete_now(i))) return fold_fail(x, F, st);
+    std::map<const void*, std::vector<std::pair<int, BatchItem>>> groups;
+    for (int i = 0; i < n; i++) {
+      if (!reduce[i]) continue;
+      ObjectPtr src;
+      std::vector<ObjectPtr> refs;
+      if ((st = resolve(x, &p[i], &bounds[i], &src, &refs, true))) return fold_fail(x, F, st);
+      BatchItem it;
+      it.id = bounds[i].id;
+      it.src = src;
+      it.b = bounds[i];
+      it.refs = refs;
+      if ((st = plan_star(x, bounds[i], src, refs, &it.plan))) return fold_fail(x, F, st);
+      bool eligible = !it.plan.empty_src && !it.plan.needs_prog;
+      for (int m = 0; m < it.plan.nmet; m++) eligible &= it.plan.wide[m] != 0;
+      if (!eligible) {
+        if ((st = complete_now(i))) return fold_fail(x, F, st);
+        continue;
+      }
+      groups[src->storage[0].get()].push_back({i, std::move(it)});
+    }
+    size_t words = 0;  // pinned bounds used so far
+    for (auto& g : groups) {
+      auto& tagged = g.second;
+      std::vector<BatchItem> items;
+      for (auto& t : tagged) items.push_back(std::move(t.second));
+      const int policy = x->cfg.batch_policy;
+      if (policy == SVM_BATCH_NEVER || (policy == SVM_BATCH_AUTO && !batch_is_cheaper(items))) {
+        for (auto& t : tagged)
+          if ((st = complete_now(t.first))) return fold_fail(x, F, st);
+        continue;
+      }
+      for (size_t b0 = 0; b0 < items.size(); b0 += 1024) {
+        const size_t b1 = std::min(items.size(), b0 + 1024);
+        std::vector<BatchItem> part(items.begin() + (long)b0, items.begin() + (long)b1);
+        FoldPart fp;
+        fp.host_off = words;
+        if ((st = exec_batch(x, part, &fp, (unsigned long long*)F->bounds.p + words))) return fold_fail(x, F, st);
+        words += (size_t)fp.nq + 2;
+        const int pi = (int)F->parts.size();
+        for (size_t j = 0; j < fp.order.size(); j++) {
+          Fold::Res& r = F->res[tagged[b0 + (size_t)fp.order[j]].first];
+          r.part = pi;
+          r.pos = (int)j;
+        }
+        F->parts.push_back(std::move(fp));
+      }
+    }
+  }
+  cudaError_t e = cudaSuccess;
+  if (F->want_host) {
+    // Every part's whole store (36 bytes a group), then each completed
+    // result's columns in its host layout.
+    size_t total = 0;
+    for (const FoldPart& fp : F->parts) {
+      F->part_stage.push_back(total);
+      F->part_groups.push_back(fp.store->nrows);
+      total += 36 * (size_t)fp.store->nrows;
+    }
+    for (Fold::Res& r : F->res) {
+      if (!r.done) continue;
+      for (int c = 0; c < r.done->ncols; c++)
+        if (r.done->is_string(c)) return fold_fail(x, F, x->fail(SVM_E_UNSUPPORTED, "fold read: " + r.id +
+                                                                 " has a String column (read it with svm_object_read)"));
+      r.stage_off = total;
+      total += host_bytes(r.done->types, r.done->nrows);
+    }
+    if ((st = x->pinned_take(total + 8, &F->stage))) return fold_fail(x, F, st);
+    char* stage = (char*)F->stage.p;
+    for (size_t pi = 0; pi < F->parts.size() && !e; pi++) {
+      const ObjectPtr& all = F->parts[pi].store;
+      const size_t G = all->nrows;
+      for (int c = 0; c < 6 && !e && G; c++) {
+        const size_t off = F->part_stage[pi] + (c < 3 ? 4 * G * c : 12 * G + 8 * G * (c - 3));
+        e = cudaMemcpyAsync(stage + off, all->col(c), G * (c < 3 ? 4 : 8), cudaMemcpyDeviceToHost, x->stream);
+      }
+    }
+    for (Fold::Res& r : F->res) {
+      if (!r.done || e) continue;
+      size_t off = r.stage_off;
+      for (int c = 0; c < r.done->ncols && !e; c++) {
+        const size_t b = r.done->nrows * r.done->elem(c);
+        if (b) e = cudaMemcpyAsync(stage + off, r.done->col(c), b, cudaMemcpyDeviceToHost, x->stream);
+        off += (b + 7) & ~size_t(7);
+      }
+    }
+  }
+  if (!e) e = cudaEventCreateWithFlags(&F->done, cudaEventDisableTiming);
+  if (!e) e = cudaEventRecord(F->done, x->stream);
+  if (e) return fold_fail(x, F, x->cuda_fail(e, "fold enqueue"));
+  *out = F;
+  return SVM_OK;
+}
+
+svm_status batch_wait(Ctx* x, void* fold, void* host, unsigned long long cap, unsigned long long* nrows_out,
+                      unsigned long long* needed) {
+  Fold* F = static_cast<Fold*>(fold);
+  cudaError_t e = cudaEventSynchronize(F->done);
+  if (e) return x->cuda_fail(e, "fold wait");
+  const unsigned long long* hb = (const unsigned long long*)F->bounds.p;
+  std::vector<unsigned long long> rows(F->res.size(), 0);
+  // Results of the batched parts (their error words first).
+  for (size_t pi = 0; pi < F->parts.size(); pi++) {
+    FoldPart& fp = F->parts[pi];
+    const unsigned long long* b = hb + fp.host_off;
+    const int err = (int)(uint32_t)b[fp.nq + 1];
+    if (err) {
+      const char* m;
+      const svm_status s = device_error_status(err, &m);
+      return x->fail(s, std::string("batch: ") + m);
+    }
+    if (!fp.items.empty()) {
+      svm_status st = store_batch_results(x, fp.items, fp.order, fp.store, b);
+      if (st) return st;
+      fp.items.clear();  // results stored once
+    }
+  }
+  unsigned long long total = 0;
+  for (size_t i = 0; i < F->res.size(); i++) {
+    const Fold::Res& r = F->res[i];
+    if (r.part >= 0) {
+      const unsigned long long* b = hb + F->parts[r.part].host_off;
+      rows[i] = b[r.pos + 1] - b[r.pos];
+      ObjectPtr o = x->find(r.id);
+      total += o ? host_bytes(o->types, rows[i]) : 0;
+    } else if (r.done) {
+      rows[i] = r.done->nrows;
+      total += host_bytes(r.done->types, rows[i]);
+    }
+    if (nrows_out) nrows_out[i] = rows[i];
+  }
+  if (needed) *needed = F->want_host ? total : 0;
+  if (!host) return SVM_OK;
+  if (!F->want_host) return x->fail(SVM_E_INVALID_ARG, "fold read: results were not staged (want_host 0)");
+  if (cap < total) return x->fail(SVM_E_INVALID_ARG, "fold read: host buffer smaller than needed bytes");
+  char* out = (char*)host;
+  const char* stage = (const char*)F->stage.p;
+  for (size_t i = 0; i < F->res.size(); i++) {
+    const Fold::Res& r = F->res[i];
+    if (r.part >= 0) {
+      const unsigned long long* b = hb + F->parts[r.part].host_off;
+      const unsigned long long row0 = b[r.pos], G = F->part_groups[r.part];
+      ObjectPtr o = x->find(r.id);
+      const int nk = (int)std::count(o->types.begin(), o->types.end(), SVM_INT32);
+      const size_t base = F->part_stage[r.part];
+      for (int c = 0; c < o->ncols; c++) {
+        const bool key = c < nk;
+        const size_t col = key ? (size_t)c : 3 + (size_t)(c - nk);
+        const size_t w = key ? 4 : 8;
+        const size_t off = base + (col < 3 ? 4 * G * col : 12 * G + 8 * G * (col - 3)) + w * row0;
+        std::memcpy(out, stage + off, w * rows[i]);
+        out += (w * rows[i] + 7) & ~size_t(7);
+      }
+    } else if (r.done) {
+      const size_t b = host_bytes(r.done->types, rows[i]);
+      std::memcpy(out, stage + r.stage_off, b);
+      out += b;
+    }
+  }
+  return SVM_OK;
+}
+
+void fold_sync(void* fold) {
+  Fold* F = static_cast<Fold*>(fold);
+  if (F && F->done) cudaEventSynchronize(F->done);
+}
+
+void batch_discard(Ctx* x, void* fold) {
+  Fold* F = static_cast<Fold*>(fold);
+  if (!F) return;
+  if (F->done) cudaEventSynchronize(F->done);
+  x->pinned_give(&F->bounds);
+  x->pinned_give(&F->stage);
+  if (F->done) cudaEventDestroy(F->done);
+  delete F;
 }
 
 }  // namespace svm

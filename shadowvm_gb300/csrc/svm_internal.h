@@ -179,6 +179,7 @@ struct StarParams {
   // appended to a per-warp buffer and aggregated 32 rows at a time.
   int agg_words;                    // words per buffered row; 0 = aggregate in place
   int8_t agg_src[kMaxDims + kMaxSteps];  // word k: probe word of dim d (0..3), or fact slot 8 + s
+  int8_t agg_step[kMaxDims + kMaxSteps]; // word k: index of the step probing that dim, or fact slot 8 + s
   Extract kx_e[kMaxKeys], xa_e[kMaxMetrics], xb_e[kMaxMetrics];  // the extractors over those words
 };
 
@@ -367,6 +368,13 @@ inline void flatten_plan(StarParams& P) {
     const Metric& M = P.metrics[m];
     P.xa_e[m] = word_of(M.xa);
     if (M.form != MF_OPND) P.xb_e[m] = word_of(M.xb);
+  }
+  for (int k = 0; k < P.agg_words; k++) {
+    const int code = P.agg_src[k];
+    P.agg_step[k] = (int8_t)code;
+    if (code < 8)
+      for (int s = 0; s < P.nsteps; s++)
+        if (P.steps[s].kind == STEP_PROBE && P.steps[s].dim == code) P.agg_step[k] = (int8_t)s;
   }
 }
 

@@ -212,6 +212,14 @@ class Engine:
         p = pipes if isinstance(pipes, Prepared) else Prepared(pipes)
         self._check(self.lib.svm_run_batch(self.h, p.n, p.arr))
 
+    def batch_begin(self, pipes, host_results: bool = False) -> "Fold":
+        """Enqueues a fold without waiting for its device work
+        (svm_batch_begin); complete it with Fold.wait / Fold.release."""
+        p = pipes if isinstance(pipes, Prepared) else Prepared(pipes)
+        h = ctypes.c_void_p()
+        self._check(self.lib.svm_batch_begin(self.h, p.n, p.arr, int(host_results), ctypes.byref(h)))
+        return Fold(self, h, p)
+
     def footprint(self, pipe) -> int:
         """Device bytes running `pipe` needs beyond what is resident (plans it;
         joined dimension tables are built and cached)."""
@@ -266,6 +274,62 @@ def capi_type(dtype) -> int:
     if dt == np.int64:
         return int(ValType.Int64)
     raise TypeError(f"unsupported column dtype {dt}")
+
+
+class Fold:
+    """A fold in flight (svm_batch_begin .. svm_batch_release)."""
+
+    def __init__(self, engine: "Engine", handle: ctypes.c_void_p, prepared: "Prepared"):
+        self.engine = engine
+        self.h = handle
+        self.prepared = prepared  # the marshalled pipelines stay alive while the fold is in flight
+        self.rows = None
+        self.needed = 0
+
+    def wait(self) -> list[int]:
+        """Blocks until the fold's device work is done; stores its results as
+        objects; returns each pipeline's row count (input order)."""
+        n = self.prepared.n
+        rows = (ctypes.c_ulonglong * max(n, 1))()
+        need = ctypes.c_ulonglong()
+        self.engine._check(self.engine.lib.svm_batch_wait(self.engine.h, self.h, rows, ctypes.byref(need)))
+        self.rows = [rows[i] for i in range(n)]
+        self.needed = need.value
+        return self.rows
+
+    def release(self, types: list[list[int]] | None = None) -> list[list[np.ndarray]] | None:
+        """Frees the fold; with `types` (each pipeline's column types, after a
+        successful wait of a fold begun with host_results) returns every
+        result's columns, copied from the fold's staging."""
+        if self.h is None:
+            return None
+        lib, eh = self.engine.lib, self.engine.h
+        if types is None or self.rows is None:
+            st = lib.svm_batch_release(eh, self.h, None, 0)
+            self.h = None
+            self.engine._check(st)
+            return None
+        buf = np.empty(max(self.needed, 8), np.uint8)
+        st = lib.svm_batch_release(eh, self.h, buf.ctypes.data_as(ctypes.c_void_p), buf.nbytes)
+        self.h = None
+        self.engine._check(st)
+        out, off = [], 0
+        for k, ts in enumerate(types):
+            cols = []
+            for t in ts:
+                dt = np.int64 if t == ValType.Int64 else np.int32
+                nb = self.rows[k] * np.dtype(dt).itemsize
+                cols.append(buf[off:off + nb].view(dt).copy())
+                off += (nb + 7) & ~7
+            out.append(cols)
+        return out
+
+    def __del__(self):
+        try:
+            if self.h is not None:
+                self.engine.lib.svm_batch_release(self.engine.h, self.h, None, 0)
+        except Exception:
+            pass
 
 
 class Prepared:

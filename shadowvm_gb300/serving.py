@@ -2,18 +2,22 @@
 engine (service/service.cu:25-63 runs one synchronous RPC at a time, with no
 batching and no admission control).
 
-A `BatchLoop` owns a worker thread.  Requests from any thread are queued with
-their arrival time.  Whenever the worker is free it takes everything that has
-arrived, admits requests in arrival order while the context's resident bytes
-plus the admitted requests' footprints (svm_pipeline_footprint: group slots,
-finalize scratch, the largest result) stay within the HBM budget, and runs
-them: one svm_run_batch launch for the fold (or one launch per request when
-the fold is small, or in serial mode).  Requests that arrive while a fold is
-on the GPU wait for the next fold, so a fold is never a fixed-size batch and
-the device stays busy while requests keep arriving.  A request over budget
-waits until memory frees up; one that can never fit fails with the budget
-error.  If a fold fails, its requests run one by one so that each gets its
-own result or error.
+A `BatchLoop` owns two worker threads.  Requests from any thread are queued
+with their arrival time.  The launcher takes everything that has arrived,
+admits requests in arrival order while the context's resident bytes plus the
+admitted requests' footprints (svm_pipeline_footprint: group slots, finalize
+scratch, the largest result) stay within the HBM budget, and begins a fold:
+svm_batch_begin plans the fold and enqueues its batched launch without
+waiting for it.  The completer waits for each fold in order
+(svm_batch_wait), copies its results out of the fold's staging and completes
+the requests.  So while one fold runs on the GPU, the requests that arrived
+meanwhile are already being admitted and planned into the next fold, which
+the device starts as soon as the running one ends: work that arrives during
+a fold overlaps it, and at most `inflight` folds are begun and not yet
+complete.  A request over budget waits until memory frees up; one that can
+never fit fails with the budget error.  If a fold fails, its requests run one
+by one so that each gets its own result or error.  Small folds and serial
+mode run one launch per request.
 
 `poisson_run` drives a loop with a seeded Poisson arrival stream and reports
 queries/s and latency percentiles (latency = completion time minus scheduled
@@ -23,6 +27,7 @@ from __future__ import annotations
 
 import collections
 import concurrent.futures as cf
+import queue
 import threading
 import time
 
@@ -57,7 +62,7 @@ class BatchLoop:
     device (a benchmark of a long stream would otherwise keep every result)."""
 
     def __init__(self, engine, budget_bytes: int = DEFAULT_BUDGET, max_fold: int = 1024, min_fold: int = 3,
-                 serial: bool = False, fetch: bool = False, drop_results: bool = False):
+                 serial: bool = False, fetch: bool = False, drop_results: bool = False, inflight: int = 2):
         self.engine = engine
         self.budget = budget_bytes
         self.max_fold = max_fold
@@ -65,13 +70,24 @@ class BatchLoop:
         self.serial = serial
         self.fetch = fetch
         self.drop_results = drop_results
+        self.inflight = max(1, inflight)
         self.folds = []                 # size of every fold run (statistics)
         self._pending = collections.deque()
         self._cv = threading.Condition()
         self._stop = False
         self._known = set()
+        self._async = hasattr(engine, "batch_begin") and self.inflight > 1
+        # folds begun and handed to the completer, in order; a slot is taken
+        # before a fold is begun and given back once it is complete, so at
+        # most `inflight` folds are begun and not complete
+        self._begun = queue.Queue()
+        self._slots = threading.Semaphore(self.inflight)
         self._thread = threading.Thread(target=self._run, name="svm-batch-loop", daemon=True)
         self._thread.start()
+        self._completer = None
+        if self._async:
+            self._completer = threading.Thread(target=self._complete, name="svm-batch-complete", daemon=True)
+            self._completer.start()
 
     # ---------------------------------------------------------------- API
     def register(self, *ids: str):
@@ -106,6 +122,9 @@ class BatchLoop:
             self._stop = True
             self._cv.notify()
         self._thread.join()
+        if self._completer is not None:
+            self._begun.put(None)
+            self._completer.join()
 
     def __enter__(self):
         return self
@@ -209,7 +228,7 @@ class BatchLoop:
             self.folds.append(len(fold))
             for r in fold:
                 r.fold = len(self.folds)
-            if self.serial or len(fold) < self.min_fold:
+            if self.serial or (not self._async and len(fold) < self.min_fold):
                 for r in fold:
                     self._run_one(r)
                 continue
@@ -217,6 +236,17 @@ class BatchLoop:
             batch.keep = [r.prepared for r in fold]
             batch.n = len(fold)
             batch.arr = (capi.svm_pipeline * len(fold))(*[r.prepared.arr[0] for r in fold])
+            if self._async:
+                self._slots.acquire()  # waits while `inflight` folds are begun and not complete
+                try:
+                    handle = self.engine.batch_begin(batch, host_results=self.fetch)
+                except Exception:
+                    self._slots.release()
+                    for r in fold:  # isolate: every request gets its own result or error
+                        self._run_one(r)
+                    continue
+                self._begun.put((fold, handle))
+                continue
             try:
                 self.engine.run_batch(batch)
             except Exception:
@@ -224,6 +254,41 @@ class BatchLoop:
                     self._run_one(r)
                 continue
             self._finish_fold(fold, [None] * len(fold))
+
+    def _complete(self):
+        """Completes begun folds in order: wait, results to the host, futures."""
+        while True:
+            item = self._begun.get()
+            if item is None:
+                return
+            fold, handle = item
+            try:
+                handle.wait()
+                results = handle.release([sink_types(r.pipe) for r in fold] if self.fetch else None)
+            except Exception:
+                try:
+                    handle.release()
+                except Exception:
+                    pass
+                self._slots.release()
+                for r in fold:  # isolate: every request gets its own result or error
+                    self._run_one(r)
+                continue
+            self._slots.release()
+            if self.fetch:
+                done = {r.pipe.id: split_result(c, r.key_num) for r, c in zip(fold, results)}
+                if self.drop_results:
+                    for r in fold:
+                        try:
+                            self.engine.drop(r.pipe.id)
+                        except Exception:
+                            pass
+            t = time.perf_counter()
+            for r in fold:
+                r.t_done = t
+                r.future.set_result(done[r.pipe.id] if self.fetch else r.pipe.id)
+                if not self.drop_results:
+                    self._known.add(r.pipe.id)
 
 
 def sink_types(pipe) -> list[int]:

@@ -206,3 +206,97 @@ def test_grpc_end_to_end():
             client.close()
         finally:
             server.stop(0)
+
+
+class FakeFold:
+    def __init__(self, eng, ids, host_results):
+        self.eng, self.ids, self.host = eng, ids, host_results
+        self.done = threading.Event()
+        self.error = None
+
+    def wait(self):
+        self.done.wait(10)
+        if self.error:
+            raise self.error
+        return [1] * len(self.ids)
+
+    def release(self, types=None):
+        with self.eng.lock:
+            self.eng.outstanding -= 1
+        if types is None:
+            return None
+        out = []
+        for i in self.ids:
+            v = sum(map(ord, i))
+            out.append([np.array([v % 7], np.int32), np.array([v], np.int64)])
+        return out
+
+
+class FakeAsyncEngine(FakeEngine):
+    """A device that runs begun folds one after another, `delay` each."""
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        import queue
+        self.q = queue.Queue()
+        self.outstanding = 0
+        self.max_outstanding = 0
+        self.log = []  # (event, fold index, time)
+        threading.Thread(target=self._device, daemon=True).start()
+
+    def _device(self):
+        while True:
+            k, f = self.q.get()
+            time.sleep(self.delay)
+            if any(i in self.fail_ids for i in f.ids):
+                f.error = SvmError(capi.E_DEVICE, "fold failed")
+            else:
+                self.objects.update(f.ids)
+            self.log.append(("done", k, time.perf_counter()))
+            f.done.set()
+
+    def batch_begin(self, prepared, host_results=False):
+        ids = self._ids(prepared)
+        with self.lock:
+            self.outstanding += 1
+            self.max_outstanding = max(self.max_outstanding, self.outstanding)
+            k = len(self.batches)
+            self.batches.append(ids)
+        self.log.append(("begin", k, time.perf_counter()))
+        f = FakeFold(self, ids, host_results)
+        self.q.put((k, f))
+        return f
+
+
+def test_folds_in_flight_overlap_and_keep_results():
+    """The next fold is begun while the previous one runs on the device; at
+    most `inflight` folds are begun and not complete; every request gets its
+    own result."""
+    eng = FakeAsyncEngine(delay=0.02)
+    with serving.BatchLoop(eng, fetch=True, inflight=2) as loop:
+        futs = {}
+        for i in range(300):
+            futs[i] = loop.submit(query(i), 1)
+            time.sleep(0.0003)
+        for i, f in futs.items():
+            keys, sums = f.result(timeout=20)
+            assert sums[0, 0] == sum(map(ord, f"q{i}"))
+    assert eng.max_outstanding <= 2
+    begins = {k: t for e, k, t in eng.log if e == "begin"}
+    dones = {k: t for e, k, t in eng.log if e == "done"}
+    overlapped = sum(1 for k in dones if k + 1 in begins and begins[k + 1] < dones[k])
+    assert overlapped >= 1, eng.log
+    assert sum(len(b) for b in eng.batches) + len(eng.singles) == 300
+
+
+def test_failed_fold_in_flight_isolates_its_requests():
+    eng = FakeAsyncEngine(delay=0.01, fail_ids={"q7"})
+    with serving.BatchLoop(eng, fetch=True, inflight=2, min_fold=1) as loop:
+        futs = [loop.submit(query(i), 1) for i in range(12)]
+        for i, f in enumerate(futs):
+            if i == 7:
+                with pytest.raises(SvmError):
+                    f.result(timeout=10)
+            else:
+                assert f.result(timeout=10)[1][0, 0] == sum(map(ord, f"q{i}"))
+    assert "q7" in eng.singles  # rerun alone after its fold failed
