@@ -310,13 +310,15 @@ svm_status svm_scan_aggregate_noalloc(svm_ctx* ctx, const svm_noalloc_scan* q, i
 /* Narrows the fused scan's launch configurations for the context's later
  * queries: rows_per_lane -1 (any), 0 (the interpreted kernel) or 4 / 8 (the
  * kernel compiled for the plan's shape, with that many rows per consumer
- * lane); ring_stages 0 (any) or 2..4; tables_staged -1 (any), 0 (small
- * dimension tables probed in L2) or 1 (staged in shared memory).  The rule,
- * or with svm_config.autotune the tuner, picks among the configurations
- * left; a query none fits returns SVM_E_UNSUPPORTED.  Every configuration
- * computes the same result.  No counterpart in the reference (its launch is
- * fixed at 1024 threads a block, com/cpp/com.cu:19-20). */
-svm_status svm_pin_launch(svm_ctx* ctx, int rows_per_lane, int ring_stages, int tables_staged);
+ * lane); blocks_per_sm 0 (any) or 2..4 (the compiled kernel built for that
+ * many resident blocks per SM: 3 or 4 with 4 rows per lane, 2 with 8);
+ * ring_stages 0 (any) or 2..4; tables_staged -1 (any), 0 (small dimension
+ * tables probed in L2) or 1 (staged in shared memory).  The rule, or with
+ * svm_config.autotune the tuner, picks among the configurations left; a
+ * query none fits returns SVM_E_UNSUPPORTED.  Every configuration computes
+ * the same result.  No counterpart in the reference (its launch is fixed at
+ * 1024 threads a block, com/cpp/com.cu:19-20). */
+svm_status svm_pin_launch(svm_ctx* ctx, int rows_per_lane, int blocks_per_sm, int ring_stages, int tables_staged);
 
 /* The launch configuration of the context's last fused scan (the kernel
  * compiled for the plan's shape or the interpreted one, rows per consumer

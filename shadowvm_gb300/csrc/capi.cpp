@@ -782,15 +782,17 @@ svm_status svm_pipeline_footprint(svm_ctx* c, const svm_pipeline* p, unsigned lo
 
 unsigned long long svm_kernel_launches(void) { return svm::launches_total(); }
 
-svm_status svm_pin_launch(svm_ctx* c, int rows_per_lane, int ring_stages, int tables_staged) {
+svm_status svm_pin_launch(svm_ctx* c, int rows_per_lane, int blocks_per_sm, int ring_stages, int tables_staged) {
   if (!c) return SVM_E_INVALID_ARG;
   if (!(rows_per_lane == -1 || rows_per_lane == 0 || rows_per_lane == 4 || rows_per_lane == 8) ||
+      !(blocks_per_sm == 0 || (blocks_per_sm >= 2 && blocks_per_sm <= 4)) ||
       !(ring_stages == 0 || (ring_stages >= 2 && ring_stages <= svm::kStages)) || tables_staged < -1 ||
       tables_staged > 1)
     return SVM_E_INVALID_ARG;
   Ctx* x = C(c);
   std::lock_guard<std::recursive_mutex> g(x->mu);
   x->pin_rows = rows_per_lane;
+  x->pin_minb = blocks_per_sm;
   x->pin_stages = ring_stages;
   x->pin_staged = tables_staged;
   return SVM_OK;

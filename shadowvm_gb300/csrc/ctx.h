@@ -173,12 +173,14 @@ struct Ctx {
     bool staged = true;
     int swap = -1;
     int rows = 0;
+    int minb = 0;   // compiled kernel: the blocks per SM it is compiled for
   };
   // Pinned launch choices (svm_pin_launch): kernel rows per lane (-1: any,
-  // 0: the interpreted kernel, 4 or 8: the compiled one), ring stages (0:
-  // any), tables staged (-1: any).  A pin narrows the candidates; the rule or
+  // 0: the interpreted kernel, 4 or 8: the compiled one), the blocks per SM
+  // the compiled kernel is built for (0: any), ring stages (0: any), tables
+  // staged (-1: any).  A pin narrows the candidates; the rule or
   // the tuner picks among those left.
-  int pin_rows = -1, pin_stages = 0, pin_staged = -1;
+  int pin_rows = -1, pin_minb = 0, pin_stages = 0, pin_staged = -1;
   // Tuned star launches: plan shape -> the fastest configuration measured.
   std::map<std::string, StarLaunch> star_tune;
   std::string last_launch;                    // the last fused scan's configuration, as text

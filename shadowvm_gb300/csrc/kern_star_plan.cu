@@ -23,10 +23,15 @@
 // 32 rows at a time into shared-memory or global int64 slots.
 //
 // Rows per lane (4 or 8) set how many independent probe loads a lane has in
-// flight per step.  Lane L owns rows 4L..4L+3 of each 128-row slice of its
-// warp's rows, so every column read is one conflict-free 16-byte
-// shared-memory load per slice.
+// flight per step, and the blocks each SM is to hold (the register budget
+// the compiler gets) set how many warps wait on those loads at once.  Lane L
+// owns rows 4L..4L+3 of each 128-row slice of its warp's rows, so every
+// column read is one conflict-free 16-byte shared-memory load per slice.
+// When no probed table's entry is wider than 16 bits, the entries kept for
+// the aggregation are stored as 16-bit words, halving that part of the
+// block's shared memory.
 #include <climits>
+#include <type_traits>
 
 #include "kern_star_common.cuh"
 #include "kernels.h"
@@ -51,18 +56,48 @@ struct StepCode {
 __host__ __device__ constexpr int plan_warp_rows(int rows_per_lane) { return 32 * rows_per_lane; }
 
 // One consumer warp's survivor list: row offsets within the warp's rows and,
-// per joined dimension, each row's table entry (indexed by row offset).
-__host__ __device__ inline size_t plan_list_bytes(int ndims, int rows_per_lane) {
+// per joined dimension, each row's table entry (indexed by row offset), in
+// 16-bit words when every entry fits them.
+__host__ __device__ inline size_t plan_list_bytes(int ndims, int rows_per_lane, bool narrow) {
   const size_t wr = (size_t)plan_warp_rows(rows_per_lane);
-  return (size_t)(ndims > 0 ? ndims : 1) * wr * 4 + wr * 2;
+  return ((size_t)(ndims > 0 ? ndims : 1) * wr * (narrow ? 2 : 4) + wr * 2 + 15) & ~size_t(15);
 }
 
-template <int kR>
+template <int kR, typename PwT>
 struct PlanList {
-  uint32_t* pwb;
+  PwT* pwb;
   uint16_t* row;
-  __device__ __forceinline__ uint32_t* pw(int d) const { return pwb + d * plan_warp_rows(kR); }
+  __device__ __forceinline__ PwT* pw(int d) const { return pwb + d * plan_warp_rows(kR); }
 };
+
+// Whether every probe step's entries fit 16 bits.
+template <int A, int B, int C, int D>
+struct PlanNarrow {
+  static constexpr int bits(int code) { return ((code & 3) >= SC_SMEM) ? (1 << ((code >> 2) & 7)) : 0; }
+  static constexpr bool value = bits(A) <= 16 && bits(B) <= 16 && bits(C) <= 16 && bits(D) <= 16;
+};
+
+template <typename PwT, int kR>
+__device__ __forceinline__ void store_entries(PwT* out, int lane, const uint32_t (&e)[kR]);
+
+template <>
+__device__ __forceinline__ void store_entries<uint32_t, 4>(uint32_t* out, int lane, const uint32_t (&e)[4]) {
+  *reinterpret_cast<uint4*>(out + 4 * lane) = make_uint4(e[0], e[1], e[2], e[3]);
+}
+template <>
+__device__ __forceinline__ void store_entries<uint32_t, 8>(uint32_t* out, int lane, const uint32_t (&e)[8]) {
+  *reinterpret_cast<uint4*>(out + 4 * lane) = make_uint4(e[0], e[1], e[2], e[3]);
+  *reinterpret_cast<uint4*>(out + 128 + 4 * lane) = make_uint4(e[4], e[5], e[6], e[7]);
+}
+template <>
+__device__ __forceinline__ void store_entries<uint16_t, 4>(uint16_t* out, int lane, const uint32_t (&e)[4]) {
+  *reinterpret_cast<uint2*>(out + 4 * lane) = make_uint2(e[0] | e[1] << 16, e[2] | e[3] << 16);
+}
+template <>
+__device__ __forceinline__ void store_entries<uint16_t, 8>(uint16_t* out, int lane, const uint32_t (&e)[8]) {
+  *reinterpret_cast<uint2*>(out + 4 * lane) = make_uint2(e[0] | e[1] << 16, e[2] | e[3] << 16);
+  *reinterpret_cast<uint2*>(out + 128 + 4 * lane) = make_uint2(e[4] | e[5] << 16, e[6] | e[7] << 16);
+}
 
 // Row offset (within the warp's rows) of row j of lane `lane`.
 template <int kR>
@@ -74,9 +109,9 @@ __device__ __forceinline__ int plan_row(int lane, int j) {
 // that pass, and stores each probed row's table entry when the table has a
 // payload.  A probe's loads go out only for rows still live; all kR of them
 // are issued before any is used.
-template <int kCode, int kR>
+template <int kCode, int kR, typename PwT>
 __device__ __forceinline__ void plan_step(const Step& st, const int32_t* wstage, const uint32_t* tables,
-                                          const PlanList<kR>& L, int lane, uint32_t& mask) {
+                                          const PlanList<kR, PwT>& L, int lane, uint32_t& mask) {
   using C = StepCode<kCode>;
   constexpr int kTR = kConsumerWarps * plan_warp_rows(kR);
   const int32_t* col = wstage + st.col * kTR;
@@ -123,29 +158,25 @@ __device__ __forceinline__ void plan_step(const Step& st, const int32_t* wstage,
       e[j] = C::bits == 32 ? word[j] : (word[j] >> sh[j]) & ((1u << (C::bits & 31)) - 1u);
       live[j] = live[j] && (e[j] & 1u);
     }
-    if (C::bits > 1) {
-      uint32_t* out = L.pw(st.dim);
-#pragma unroll
-      for (int q = 0; q < kR / 4; q++)
-        *reinterpret_cast<uint4*>(out + q * 128 + 4 * lane) =
-            make_uint4(e[4 * q], e[4 * q + 1], e[4 * q + 2], e[4 * q + 3]);
-    }
+    if (C::bits > 1) store_entries<PwT, kR>(L.pw(st.dim), lane, e);
   }
   mask = 0;
 #pragma unroll
   for (int j = 0; j < kR; j++) mask |= (uint32_t)live[j] << j;
 }
 
-template <int kCode, int kR>
+template <int kCode, int kR, typename PwT>
 __device__ __forceinline__ void plan_step_if(const Step& st, const int32_t* wstage, const uint32_t* tables,
-                                             const PlanList<kR>& L, int lane, uint32_t& mask) {
+                                             const PlanList<kR, PwT>& L, int lane, uint32_t& mask) {
   if (kCode == SC_NONE) return;
   if (!__any_sync(0xffffffffu, mask)) return;
-  plan_step<kCode, kR>(st, wstage, tables, L, lane, mask);
+  plan_step<kCode, kR, PwT>(st, wstage, tables, L, lane, mask);
 }
 
-template <int kAgg, int kR, int S0, int S1, int S2, int S3>
-__global__ void __launch_bounds__(kStarThreads, kR == 4 ? 3 : 2) star_plan_kernel(const __grid_constant__ StarParams P) {
+template <int kAgg, int kR, int kMinB, int S0, int S1, int S2, int S3>
+__global__ void __launch_bounds__(kStarThreads, kMinB) star_plan_kernel(const __grid_constant__ StarParams P) {
+  constexpr bool kNarrow = PlanNarrow<S0, S1, S2, S3>::value;
+  using PwT = typename std::conditional<kNarrow, uint16_t, uint32_t>::type;
   constexpr int kWR = plan_warp_rows(kR);
   constexpr int kTR = kConsumerWarps * kWR;
   extern __shared__ __align__(128) uint8_t dyn[];
@@ -153,7 +184,7 @@ __global__ void __launch_bounds__(kStarThreads, kR == 4 ? 3 : 2) star_plan_kerne
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ncols = P.ncols, nst = P.nstages;
   int32_t* ring = reinterpret_cast<int32_t*>(dyn);
-  const size_t lb = plan_list_bytes(P.ndims, kR);
+  const size_t lb = plan_list_bytes(P.ndims, kR, kNarrow);
   uint8_t* lists = dyn + (size_t)nst * ncols * kTR * 4;
   uint32_t* tables = reinterpret_cast<uint32_t*>(lists + kConsumerWarps * lb);
   unsigned long long* s_sum =
@@ -212,9 +243,10 @@ __global__ void __launch_bounds__(kStarThreads, kR == 4 ? 3 : 2) star_plan_kerne
     }
   } else {
     // ---------------- consumers
-    PlanList<kR> L;
-    L.pwb = reinterpret_cast<uint32_t*>(lists + (size_t)warp * lb);
-    L.row = reinterpret_cast<uint16_t*>(lists + (size_t)warp * lb + (size_t)(P.ndims > 0 ? P.ndims : 1) * kWR * 4);
+    PlanList<kR, PwT> L;
+    L.pwb = reinterpret_cast<PwT*>(lists + (size_t)warp * lb);
+    L.row = reinterpret_cast<uint16_t*>(lists + (size_t)warp * lb +
+                                        (size_t)(P.ndims > 0 ? P.ndims : 1) * kWR * sizeof(PwT));
     const uint32_t lt = lanemask_lt();
     const int W = P.agg_words;
     uint32_t* buf = aggbuf + (size_t)warp * kAggCap * W;
@@ -239,10 +271,10 @@ __global__ void __launch_bounds__(kStarThreads, kR == 4 ? 3 : 2) star_plan_kerne
           mask |= (uint32_t)(r >= P.row_begin && r < P.row_end) << j;
         }
       }
-      plan_step_if<S0, kR>(P.steps[0], wstage, tables, L, lane, mask);
-      plan_step_if<S1, kR>(P.steps[1], wstage, tables, L, lane, mask);
-      plan_step_if<S2, kR>(P.steps[2], wstage, tables, L, lane, mask);
-      plan_step_if<S3, kR>(P.steps[3], wstage, tables, L, lane, mask);
+      plan_step_if<S0, kR, PwT>(P.steps[0], wstage, tables, L, lane, mask);
+      plan_step_if<S1, kR, PwT>(P.steps[1], wstage, tables, L, lane, mask);
+      plan_step_if<S2, kR, PwT>(P.steps[2], wstage, tables, L, lane, mask);
+      plan_step_if<S3, kR, PwT>(P.steps[3], wstage, tables, L, lane, mask);
 
       // ---- the survivors as a list of row offsets
       int n = 0;
@@ -261,7 +293,7 @@ __global__ void __launch_bounds__(kStarThreads, kR == 4 ? 3 : 2) star_plan_kerne
           uint32_t* ent = buf + (size_t)(cnt + lane) * W;
           for (int k = 0; k < W; k++) {
             const int code = P.agg_src[k];
-            ent[k] = code < 8 ? L.pw(code)[row] : (uint32_t)wstage[(code - 8) * kTR + row];
+            ent[k] = code < 8 ? (uint32_t)L.pw(code)[row] : (uint32_t)wstage[(code - 8) * kTR + row];
           }
         }
         cnt += take;
@@ -285,13 +317,15 @@ constexpr int smem(int bits_log2) { return SC_SMEM | bits_log2 << 2; }
 constexpr int l2(int bits_log2) { return SC_L2 | bits_log2 << 2; }
 
 struct PlanEntry {
-  int agg, rows, s[4];
+  int agg, rows, minb, s[4];
   const void* fn;
 };
 
-#define SVM_PLAN(AGG, R, A, B, C, D) \
-  {AGG, R, {A, B, C, D}, reinterpret_cast<const void*>(&star_plan_kernel<AGG, R, A, B, C, D>)}
-#define SVM_PLAN_R(AGG, A, B, C, D) SVM_PLAN(AGG, 4, A, B, C, D), SVM_PLAN(AGG, 8, A, B, C, D)
+#define SVM_PLAN(AGG, R, MB, A, B, C, D) \
+  {AGG, R, MB, {A, B, C, D}, reinterpret_cast<const void*>(&star_plan_kernel<AGG, R, MB, A, B, C, D>)}
+// Each shape with 4 rows per lane for 3 or 4 blocks per SM, and 8 rows per lane for 2.
+#define SVM_PLAN_R(AGG, A, B, C, D) \
+  SVM_PLAN(AGG, 4, 3, A, B, C, D), SVM_PLAN(AGG, 4, 4, A, B, C, D), SVM_PLAN(AGG, 8, 2, A, B, C, D)
 
 // Shapes the planner produces for the star-schema workloads, each with its
 // small tables staged in shared memory and probed in L2:
@@ -325,7 +359,7 @@ bool plan_is_compilable(const StarParams& p) {
   return true;
 }
 
-const PlanEntry* find_plan(const StarParams& p, int rows) {
+const PlanEntry* find_plan(const StarParams& p, int rows, int minb) {
   if (!plan_is_compilable(p)) return nullptr;
   int code[4];
   for (int k = 0; k < 4; k++) {
@@ -333,8 +367,8 @@ const PlanEntry* find_plan(const StarParams& p, int rows) {
     if (code[k] < 0) return nullptr;
   }
   for (const PlanEntry& e : kPlans)
-    if (e.agg == p.agg && e.rows == rows && e.s[0] == code[0] && e.s[1] == code[1] && e.s[2] == code[2] &&
-        e.s[3] == code[3])
+    if (e.agg == p.agg && e.rows == rows && e.minb == minb && e.s[0] == code[0] && e.s[1] == code[1] &&
+        e.s[2] == code[2] && e.s[3] == code[3])
       return &e;
   return nullptr;
 }
@@ -352,12 +386,17 @@ int star_plan_code(const StarParams& p, int k) {
   return (st.smem_word_off >= 0 ? SC_SMEM : SC_L2) | lg << 2 | (ranged ? 32 : 0);
 }
 
-bool star_plan_available(const StarParams& p, int rows_per_lane) { return find_plan(p, rows_per_lane) != nullptr; }
+bool star_plan_available(const StarParams& p, int rows_per_lane, int min_blocks) {
+  return find_plan(p, rows_per_lane, min_blocks) != nullptr;
+}
 
 size_t star_plan_smem_bytes(const StarParams& p, int rows_per_lane) {
   const size_t tr = (size_t)kConsumerWarps * plan_warp_rows(rows_per_lane);
+  bool narrow = true;
+  for (int k = 0; k < p.nsteps; k++)
+    if (p.steps[k].kind == STEP_PROBE && p.steps[k].entry_bits > 16) narrow = false;
   size_t b = (size_t)p.nstages * p.ncols * tr * 4;
-  b += plan_list_bytes(p.ndims, rows_per_lane) * kConsumerWarps;
+  b += plan_list_bytes(p.ndims, rows_per_lane, narrow) * kConsumerWarps;
   b += (size_t)((p.smem_table_words + 3) & ~3) * 4;
   if (p.agg == AGG_DENSE_SMEM) b += (size_t)p.ngroups * (8 * p.nmetrics + 4);
   b = (b + 15) & ~size_t(15);
@@ -365,8 +404,8 @@ size_t star_plan_smem_bytes(const StarParams& p, int rows_per_lane) {
   return b;
 }
 
-int star_plan_blocks_per_sm(const StarParams& p, int rows_per_lane, size_t smem) {
-  const PlanEntry* e = find_plan(p, rows_per_lane);
+int star_plan_blocks_per_sm(const StarParams& p, int rows_per_lane, int min_blocks, size_t smem) {
+  const PlanEntry* e = find_plan(p, rows_per_lane, min_blocks);
   if (!e) return 0;
   if (allow_dynamic_smem(e->fn, 210 * 1024) != cudaSuccess) return 0;
   int per_sm = 0;
@@ -374,8 +413,8 @@ int star_plan_blocks_per_sm(const StarParams& p, int rows_per_lane, size_t smem)
   return per_sm;
 }
 
-int star_plan_grid_size(const StarParams& p, int rows_per_lane, size_t smem) {
-  int per_sm = star_plan_blocks_per_sm(p, rows_per_lane, smem);
+int star_plan_grid_size(const StarParams& p, int rows_per_lane, int min_blocks, size_t smem) {
+  int per_sm = star_plan_blocks_per_sm(p, rows_per_lane, min_blocks, smem);
   if (per_sm < 1) per_sm = 1;
   const long long tr = (long long)kConsumerWarps * plan_warp_rows(rows_per_lane);
   long long tiles = (p.row_end - (p.row_begin & ~3ll) + tr - 1) / tr;
@@ -384,8 +423,9 @@ int star_plan_grid_size(const StarParams& p, int rows_per_lane, size_t smem) {
   return (int)(tiles < cap ? tiles : cap);
 }
 
-cudaError_t launch_star_plan(const StarParams& p, int rows_per_lane, int grid, size_t smem, cudaStream_t s) {
-  const PlanEntry* e = find_plan(p, rows_per_lane);
+cudaError_t launch_star_plan(const StarParams& p, int rows_per_lane, int min_blocks, int grid, size_t smem,
+                             cudaStream_t s) {
+  const PlanEntry* e = find_plan(p, rows_per_lane, min_blocks);
   if (!e) return cudaErrorInvalidValue;
   note_launch();
   void* args[] = {const_cast<StarParams*>(&p)};

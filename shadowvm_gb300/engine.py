@@ -238,10 +238,11 @@ class Engine:
         return keys, mets
 
     # ------------------------------------------------------------ profiling
-    def pin_launch(self, rows_per_lane: int = -1, ring_stages: int = 0, tables_staged: int = -1):
+    def pin_launch(self, rows_per_lane: int = -1, ring_stages: int = 0, tables_staged: int = -1,
+                   blocks_per_sm: int = 0):
         """Narrows the fused scan's launch configurations (svm_pin_launch);
         the defaults lift every pin."""
-        self._check(self.lib.svm_pin_launch(self.h, rows_per_lane, ring_stages, tables_staged))
+        self._check(self.lib.svm_pin_launch(self.h, rows_per_lane, blocks_per_sm, ring_stages, tables_staged))
 
     def last_launch(self) -> dict:
         """The last fused scan's launch configuration (svm_last_launch)."""

@@ -3,7 +3,8 @@
 Each golden case (the reference's own results for configs 0, 1, 2 and 5 at
 test scale, including a dimension the capped insert drops keys from) runs
 under every pinned choice the tuner varies: the kernel compiled for the
-plan's shape with 4 or 8 rows per consumer lane, or the interpreted kernel;
+plan's shape with 4 rows per consumer lane (built for 3 or 4 blocks per SM)
+or 8 (for 2), or the interpreted kernel;
 2 or 3 ring stages; small tables staged in shared memory or probed in L2.
 Every variant must equal the golden rows bit for bit, and the shapes of
 configs 0, 1 and 2 must have a compiled kernel (the launch reports it)."""
@@ -42,10 +43,10 @@ def test_every_launch_variant_equals_the_reference(engine_factory, name):
     for p in w.dim_pipelines:
         eng.run(p)
     kernels = set()
-    for rows in (4, 8, 0):
+    for rows, minb in ((4, 3), (4, 4), (8, 2), (0, 0)):
         for stages in (2, 3):
             for staged in (1, 0):
-                eng.pin_launch(rows, stages, staged)
+                eng.pin_launch(rows, stages, staged, blocks_per_sm=minb)
                 try:
                     eng.run(w.query)
                 except SvmError as e:
