@@ -114,6 +114,58 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def gpu_numa_node(device: int):
+    """The host NUMA node the GPU's PCI function reports (sysfs), or None."""
+    try:
+        import torch
+        pr = torch.cuda.get_device_properties(device)
+        bus = f"{pr.pci_domain_id:04x}:{pr.pci_bus_id:02x}:{pr.pci_device_id:02x}.0"
+        with open(f"/sys/bus/pci/devices/{bus}/numa_node") as f:
+            node = int(f.read().strip())
+        return node if node >= 0 else None
+    except Exception:
+        return None
+
+
+def node_cpus(node: int):
+    """CPUs of a NUMA node (sysfs cpulist), or None."""
+    try:
+        text = open(f"/sys/devices/system/node/node{node}/cpulist").read().strip()
+    except OSError:
+        return None
+    cpus = set()
+    for part in text.split(","):
+        if not part:
+            continue
+        a, _, b = part.partition("-")
+        cpus.update(range(int(a), int(b or a) + 1))
+    return cpus or None
+
+
+def pages_node(addr: int, nbytes: int, samples: int = 16):
+    """NUMA nodes of a few pages of a host buffer (move_pages with no target
+    nodes only reports where each page is); {} where the call is missing."""
+    import ctypes
+    import platform
+    nr = {"aarch64": 239, "x86_64": 279}.get(platform.machine())
+    if nr is None or nbytes <= 0:
+        return {}
+    try:
+        libc = ctypes.CDLL(None, use_errno=True)
+        page = os.sysconf("SC_PAGE_SIZE")
+        addrs = [addr + (nbytes - page) * i // max(1, samples - 1) // page * page for i in range(samples)]
+        pages = (ctypes.c_void_p * samples)(*addrs)
+        status = (ctypes.c_int * samples)()
+        if libc.syscall(nr, 0, samples, pages, None, status, 0) != 0:
+            return {}
+        out = {}
+        for v in status:
+            out[v] = out.get(v, 0) + 1
+        return out
+    except Exception:
+        return {}
+
+
 def cpu_reference_run(cfg: int, sample_rows: int, steps: int, threads: int):
     """The reference's generated CPU path (oracle port) on `sample_rows` fact rows.
     Returns (rows/s per step list, hash build ms, description)."""
@@ -285,6 +337,7 @@ def ours_arm(args):
     n_star, star_ms = eng.profile_read(capi.K_STAR)
     eng.profile(False)
     clk = clocks.stop()
+    launch_cfg = eng.last_launch()
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([ms], device="cuda")
@@ -310,12 +363,23 @@ def ours_arm(args):
     e2e = None
     if not args.no_e2e:
         used = {0: [0, 1, 2, 3], 1: [0, 4, 5], 2: [0, 5, 6, 7, 8], 5: [0, 5, 6, 7, 8]}[args.config]
+        # The page-locked columns are placed on the host NUMA node local to
+        # the GPU: the allocating thread runs on that node's CPUs while the
+        # pages are allocated, pinned and first written (host-side placement
+        # only; no GPU setting changes).
+        node = gpu_numa_node(local)
+        cpus = node_cpus(node) if node is not None else None
+        saved = os.sched_getaffinity(0)
+        if cpus:
+            os.sched_setaffinity(0, cpus & set(range(os.cpu_count() or 1)) or saved)
         pinned = {}
         for c in used:
             t = torch.empty(rows, dtype=torch.int32, pin_memory=True)
             a = t.numpy()
             a[:] = eng.read("lineorder", c)
             pinned[c] = (t, a)
+        os.sched_setaffinity(0, saved)
+        placed = pages_node(pinned[used[0]][1].ctypes.data, pinned[used[0]][1].nbytes)
         import copy
         qp = copy.deepcopy(w.query)
         qp.pre_pipeline_id[0] = "lineorder_e2e"
@@ -340,6 +404,8 @@ def ours_arm(args):
             e2e_s = float(t.item())
         e2e = {"value": rows * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+               "h2d_gb_per_s": h2d / e2e_s / 1e9,
+               "host_numa": {"gpu_node": node, "pinned_pages_on_node": {str(k): v for k, v in placed.items()}},
                "api": "svm_object_put (pinned host columns) + svm_run_pipeline + svm_object_read"}
         eng.drop("lineorder_e2e")
 
@@ -385,6 +451,7 @@ def ours_arm(args):
                "config": dict(workload_config(args.config, rows * world), join_mode=args.join_mode,
                               rows_per_gpu=rows, parallelism=f"row shards x{world}"),
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+               "launch": launch_cfg,
                "clocks": clk, "dimension_build_s": build_s,
                "hbm_frac_of_measured": roofline["frac"], "parity": parity, "batched": batched}
         print(json.dumps(out))
@@ -494,7 +561,7 @@ def served_arm(args):
     import dataclasses
 
     import torch
-    from shadowvm_gb300 import Engine, serving
+    from shadowvm_gb300 import Engine, capi, serving
     from shadowvm_gb300 import workloads as W
     rank, world, local = rank_info()
     if rank != 0:
@@ -523,9 +590,14 @@ def served_arm(args):
     points = {"batched": [], "serial": []}
     for rate in rates:
         for mode in ("batched", "serial"):
+            eng.profile(True)
+            eng.profile_reset()
             with serving.BatchLoop(eng, budget_bytes=150 * 10**9, serial=(mode == "serial"), fetch=True,
-                                   drop_results=True) as loop:
+                                   drop_results=True, max_fold=args.max_fold, inflight=args.inflight) as loop:
                 r = serving.poisson_run(loop, make_pipe, rate, args.serve_seconds, seed=int(rate))
+            r["device_s"] = {name: eng.profile_read(k)[1] / 1e3 for name, k in
+                             (("batch", capi.K_BATCH), ("star", capi.K_STAR), ("finalize", capi.K_FINALIZE))}
+            eng.profile(False)
             points[mode].append(r)
     clk = clocks.stop()
 
@@ -643,6 +715,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the config-3 batched measurement")
     ap.add_argument("--rates", default="100,1000,2500,5000", help="config 4: offered queries/s")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="config 4: seconds of arrivals per point")
+    ap.add_argument("--max-fold", type=int, default=1024, help="config 4: most requests in one fold")
+    ap.add_argument("--inflight", type=int, default=2, help="config 4: folds begun and not complete, at most")
     ap.add_argument("--loader", action="store_true", help="measure the text Loader instead")
     ap.add_argument("--join-mode", default="ref_compat", choices=["ref_compat", "exact"])
     args = ap.parse_args()

@@ -72,6 +72,9 @@ class BatchLoop:
         self.drop_results = drop_results
         self.inflight = max(1, inflight)
         self.folds = []                 # size of every fold run (statistics)
+        # seconds spent per phase (statistics): launcher admit / slot wait /
+        # begin, completer wait / release / finish
+        self.phase_s = collections.Counter()
         self._pending = collections.deque()
         self._cv = threading.Condition()
         self._stop = False
@@ -222,7 +225,9 @@ class BatchLoop:
             reqs = self._take()
             if reqs is None:
                 return
+            t0 = time.perf_counter()
             fold = self._admit(reqs)
+            self.phase_s["admit"] += time.perf_counter() - t0
             if not fold:
                 continue
             self.folds.append(len(fold))
@@ -237,7 +242,10 @@ class BatchLoop:
             batch.n = len(fold)
             batch.arr = (capi.svm_pipeline * len(fold))(*[r.prepared.arr[0] for r in fold])
             if self._async:
+                t2 = time.perf_counter()
                 self._slots.acquire()  # waits while `inflight` folds are begun and not complete
+                t3 = time.perf_counter()
+                self.phase_s["slot_wait"] += t3 - t2
                 try:
                     handle = self.engine.batch_begin(batch, host_results=self.fetch)
                 except Exception:
@@ -245,6 +253,7 @@ class BatchLoop:
                     for r in fold:  # isolate: every request gets its own result or error
                         self._run_one(r)
                     continue
+                self.phase_s["begin"] += time.perf_counter() - t3
                 self._begun.put((fold, handle))
                 continue
             try:
@@ -263,8 +272,12 @@ class BatchLoop:
                 return
             fold, handle = item
             try:
+                t0 = time.perf_counter()
                 handle.wait()
+                t1 = time.perf_counter()
                 results = handle.release([sink_types(r.pipe) for r in fold] if self.fetch else None)
+                self.phase_s["wait"] += t1 - t0
+                self.phase_s["release"] += time.perf_counter() - t1
             except Exception:
                 try:
                     handle.release()
@@ -289,6 +302,7 @@ class BatchLoop:
                 r.future.set_result(done[r.pipe.id] if self.fetch else r.pipe.id)
                 if not self.drop_results:
                     self._known.add(r.pipe.id)
+            self.phase_s["finish"] += time.perf_counter() - t
 
 
 def sink_types(pipe) -> list[int]:
@@ -313,14 +327,18 @@ def poisson_run(loop: BatchLoop, make_pipe, rate: float, seconds: float, seed: i
     arrivals = np.cumsum(gaps)
     arrivals = arrivals[arrivals < seconds]
     futures = []
+    loop.phase_s.clear()
+    submit_s = 0.0
     t0 = time.perf_counter()
     i = 0
     n = len(arrivals)
     while i < n:
         now = time.perf_counter() - t0
         while i < n and arrivals[i] <= now:
+            ts = time.perf_counter()
             pipe, key_num = make_pipe(i)
             futures.append(loop.submit(pipe, key_num, t_arrival=t0 + arrivals[i]))
+            submit_s += time.perf_counter() - ts
             i += 1
         if i < n:
             time.sleep(max(0.0, min(tick, arrivals[i] - (time.perf_counter() - t0))))
@@ -339,4 +357,5 @@ def poisson_run(loop: BatchLoop, make_pipe, rate: float, seconds: float, seed: i
             "achieved_qps": len(reqs) / span if span > 0 else 0.0,
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "p999": float(np.percentile(lat, 99.9)), "max": float(lat.max())},
-            "folds": len(per_fold), "mean_fold": float(np.mean(list(per_fold.values()))) if per_fold else 0.0}
+            "folds": len(per_fold), "mean_fold": float(np.mean(list(per_fold.values()))) if per_fold else 0.0,
+            "host_s": dict(loop.phase_s, submit=submit_s)}
