@@ -343,8 +343,39 @@ class Prepared:
         self.arr = (capi.svm_pipeline * max(self.n, 1))(*[marshal(p, self.keep) for p in pipes])
 
 
+# Marshalled operator and pre_pipeline_id arrays by pipeline content (its
+# operators and inputs, not its id): a server sees the same query text again
+# and again under new ids, and building the ctypes arrays is most of the
+# cost of marshalling.  The arrays are read-only to the library, so requests
+# share them; the cache keeps them alive.
+_MARSHAL_CACHE: dict = {}
+_MARSHAL_CACHE_MAX = 4096
+
+
+def _content_key(pipe: PipelineInfo):
+    return (tuple((int(op.type), tuple(sorted(op.args.items())),
+                   tuple((int(c.type), int(c.val_size)) for c in op.output.column_list)
+                   if op.output is not None else None) for op in pipe.workflow),
+            tuple(pipe.pre_pipeline_id))
+
+
 def marshal(pipe: PipelineInfo, keep: list) -> capi.svm_pipeline:
     """PipelineInfo -> svm_pipeline; `keep` holds the buffers alive."""
+    key = _content_key(pipe)
+    hit = _MARSHAL_CACHE.get(key)
+    if hit is None:
+        hit = _marshal_ops(pipe)
+        if len(_MARSHAL_CACHE) >= _MARSHAL_CACHE_MAX:
+            _MARSHAL_CACHE.clear()
+        _MARSHAL_CACHE[key] = hit
+    ops, nops, pre, npre = hit
+    pid = pipe.id.encode()
+    keep += [hit, pid]
+    return capi.svm_pipeline(pid, nops, ops, npre, pre)
+
+
+def _marshal_ops(pipe: PipelineInfo):
+    keep = []
     ops = (capi.svm_operator * max(len(pipe.workflow), 1))()
     for i, op in enumerate(pipe.workflow):
         items = sorted(op.args.items())
@@ -355,8 +386,8 @@ def marshal(pipe: PipelineInfo, keep: list) -> capi.svm_pipeline:
         keep += [args, out]
         ops[i] = capi.svm_operator(int(op.type), len(items), args, len(cols), out)
     pre = (ctypes.c_char_p * max(len(pipe.pre_pipeline_id), 1))(*[s.encode() for s in pipe.pre_pipeline_id])
-    keep += [ops, pre]
-    return capi.svm_pipeline(pipe.id.encode(), len(pipe.workflow), ops, len(pipe.pre_pipeline_id), pre)
+    ops._keep = keep  # the operators' argument and column arrays live as long as the operator array
+    return ops, len(pipe.workflow), pre, len(pipe.pre_pipeline_id)
 
 
 def reduce_shape(pipe: PipelineInfo) -> tuple[int, int]:
