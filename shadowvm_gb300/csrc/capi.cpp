@@ -414,7 +414,7 @@ svm_status svm_object_put_columns(svm_ctx* c, const char* id, int ncols, const s
   }
   cudaError_t e = cudaStreamSynchronize(x->stream);
   if (e) return x->cuda_fail(e, "object upload");
-  x->objects[id] = o;
+  x->put_object(id, o);
   x->purge_rank_cache();
   return SVM_OK;
 }
@@ -502,7 +502,7 @@ svm_status svm_object_load_text(svm_ctx* c, const char* id, int ncols, const int
   if (!e) e = cudaStreamSynchronize(x->stream);
   if (e) return x->cuda_fail(e, "text loader parse");
   if (h) return x->fail(SVM_E_INVALID_ARG, "text loader: an item longer than 4095 bytes");
-  x->objects[id] = o;
+  x->put_object(id, o);
   if (nrows_out) *nrows_out = total.rows;
   return SVM_OK;
 }
@@ -555,7 +555,7 @@ svm_status svm_object_view(svm_ctx* c, const char* id, const char* base, unsigne
   o->bulk0_rows = nrows < x->cfg.tuple_per_bulk ? nrows : x->cfg.tuple_per_bulk;
   o->source_rows = nrows;
   // Column statistics of the base bound the view's values.
-  x->objects[id] = o;
+  x->put_object(id, o);
   return SVM_OK;
 }
 
@@ -646,7 +646,11 @@ svm_status svm_object_drop(svm_ctx* c, const char* id) {
   cudaSetDevice(x->device);
   auto it = x->objects.find(id);
   if (it == x->objects.end()) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
-  cudaStreamSynchronize(x->stream);
+  // No wait for the stream: work already enqueued that reads the object
+  // runs first, and its blocks go back to a pool whose next user is ordered
+  // behind that work on the same stream (a block too big for the pool is
+  // freed with cudaFree, which waits for the device itself).
+  x->forget_plans(it->second.get());
   x->objects.erase(it);
   x->purge_rank_cache();
   // Tables built over the dropped object are keyed by its version; drop them

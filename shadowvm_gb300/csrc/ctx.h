@@ -181,6 +181,10 @@ struct Ctx {
   // staged (-1: any).  A pin narrows the candidates; the rule or
   // the tuner picks among those left.
   int pin_rows = -1, pin_minb = 0, pin_stages = 0, pin_staged = -1;
+  // Planned fact pipelines by content and the versions of the objects they
+  // read (pipeline.cpp); forget_plans drops the plans that read `o`.
+  std::shared_ptr<void> plan_cache;
+  void forget_plans(const Object* o);
   // Tuned star launches: plan shape -> the fastest configuration measured.
   std::map<std::string, StarLaunch> star_tune;
   std::string last_launch;                    // the last fused scan's configuration, as text
@@ -219,6 +223,17 @@ struct Ctx {
   void scratch_reset() { scratch_used = 0; }
   svm_status scratch_take(size_t bytes, void** out);
   svm_status scratch_reserve(size_t bytes);
+
+  // Stores object `id`, forgetting the plans that read the object it replaces.
+  void put_object(const std::string& id, ObjectPtr o) {
+    auto it = objects.find(id);
+    if (it != objects.end()) {
+      forget_plans(it->second.get());
+      it->second = std::move(o);
+    } else {
+      objects.emplace(id, std::move(o));
+    }
+  }
 
   ObjectPtr find(const std::string& id) {
     auto it = objects.find(id);

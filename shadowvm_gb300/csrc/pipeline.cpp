@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstring>
 #include <set>
+#include <unordered_map>
 
 #include "ctx.h"
 #include "expr.h"
@@ -350,7 +351,7 @@ svm_status run_select(Ctx* x, const Bound& b, const ObjectPtr& src, const std::v
       oc.dict = truncate_dict(*in.dict, oc.width, &remap);
       DevBufPtr lut;
       if ((st = x->alloc(4 * remap.size() + 4, &lut))) return st;
-      if (!e) e = cudaMemcpy(lut->p, remap.data(), 4 * remap.size(), cudaMemcpyHostToDevice);
+      if (!e) e = cudaMemcpyAsync(lut->p, remap.data(), 4 * remap.size(), cudaMemcpyHostToDevice, x->stream);
       if (!e) e = launch_lut_gather((const int32_t*)out->col((int)i), out->nrows, (const int32_t*)lut->p,
                                     (int32_t*)out->col((int)i), x->stream);
       luts.push_back(lut);
@@ -364,7 +365,7 @@ svm_status run_select(Ctx* x, const Bound& b, const ObjectPtr& src, const std::v
   out->has_bulks = src->has_bulks;
   out->bulk0_rows = hdr[1];
   out->source_rows = src->nrows;
-  x->objects[b.id] = out;
+  x->put_object(b.id, out);
   return SVM_OK;
 }
 
@@ -866,6 +867,73 @@ svm_status plan_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::ve
   return SVM_OK;
 }
 
+// ---- plan cache
+// A server sees the same query text again and again (under new pipeline
+// ids); planning it -- parsing, column statistics, table lookups, the step
+// order -- is most of the host time per request.  Plans are kept by the
+// bound pipeline's content (after String rewriting, id excluded) and the
+// identity, version and row range of every object it reads, so a replaced
+// or regenerated object never meets a stale plan; the plans that read an
+// object are forgotten when it is dropped or replaced.
+struct PlanCache {
+  std::unordered_map<std::string, StarPlan> plans;
+  std::unordered_map<const Object*, std::vector<std::string>> by_object;
+};
+
+PlanCache* plan_cache(Ctx* x) {
+  if (!x->plan_cache) x->plan_cache = std::make_shared<PlanCache>();
+  return static_cast<PlanCache*>(x->plan_cache.get());
+}
+
+std::string plan_key(const Bound& b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs) {
+  std::string k;
+  auto add = [&](const std::string& t) {
+    k += t;
+    k += '\x1f';
+  };
+  for (auto& e : b.filter_exp) add(e);
+  k += '\x1e';
+  for (auto& e : b.metric_exp) add(e);
+  k += '\x1e';
+  for (auto* v : {&b.reduce_key, &b.join_lkey, &b.join_rkey}) {
+    for (auto& r : *v) add(std::to_string(r.obj) + "." + std::to_string(r.col));
+    k += '\x1e';
+  }
+  for (auto& c : b.sink) add(std::to_string(c.type) + ":" + std::to_string(c.val_size));
+  k += '\x1e';
+  auto obj = [&](const ObjectPtr& o) {
+    add(std::to_string((uintptr_t)o.get()) + ":" + std::to_string(o->version) + ":" + std::to_string(o->row0) + ":" +
+        std::to_string(o->nrows));
+  };
+  obj(src);
+  for (auto& r : refs) obj(r);
+  return k;
+}
+
+svm_status plan_star_cached(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs,
+                            StarPlan* plan) {
+  PlanCache* pc = plan_cache(x);
+  const std::string key = plan_key(b, src, refs);
+  auto hit = pc->plans.find(key);
+  if (hit != pc->plans.end()) {
+    *plan = hit->second;
+    plan->P.error = x->d_error;
+    plan->P.wait_polls = x->wait_polls;
+    plan->P.stall_copies = x->stall_copies;
+    return SVM_OK;
+  }
+  svm_status st = plan_star(x, b, src, refs, plan);
+  if (st) return st;
+  if (pc->plans.size() >= 4096) {
+    pc->plans.clear();
+    pc->by_object.clear();
+  }
+  pc->plans.emplace(key, *plan);
+  pc->by_object[src.get()].push_back(key);
+  for (auto& r : refs) pc->by_object[r.get()].push_back(key);
+  return SVM_OK;
+}
+
 // The shape a star launch is tuned for: columns, steps (kind, table layout,
 // placement, entry width), dimensions, aggregation, and the orders of
 // magnitude of the group count and the rows scanned.
@@ -916,7 +984,7 @@ svm_status translate_keys(Ctx* x, const Bound& b, const ObjectPtr& out) {
 
 svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vector<ObjectPtr>& refs) {
   StarPlan plan;
-  svm_status st = plan_star(x, b, src, refs, &plan);
+  svm_status st = plan_star_cached(x, b, src, refs, &plan);
   if (st) return st;
   const std::vector<int>& out_types = plan.out_types;
   const int nkeys = plan.nkeys, nmet = plan.nmet;
@@ -924,7 +992,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   if (plan.empty_src) {
     ObjectPtr out = new_result_object(x, b.id, out_types, 0, &st);
     if (st) return st;
-    x->objects[b.id] = out;
+    x->put_object(b.id, out);
     return SVM_OK;
   }
   StarParams& P = plan.P;
@@ -968,12 +1036,17 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
                                                  std::to_string(x->pin_minb) + "," + std::to_string(x->pin_stages) +
                                                  "," + std::to_string(x->pin_staged)
                                            : std::string();  // as planned
+  // The compiled kernel reads the columns no filter step needs only at the
+  // surviving rows (late columns); the interpreted kernel stages them all.
+  const StarParams P0 = P;
   auto configure = [&](const Cand& c) {
+    P = P0;
     P.nstages = c.nst;
     for (int d = 0; d < P.ndims; d++) P.dims[d].smem_word_off = c.staged ? staged_off[d] : -1;
     P.smem_table_words = c.staged ? staged_words : 0;
     for (int k = 0; k < P.nsteps; k++) P.steps[k] = steps0[k];
     if (c.swap >= 0) std::swap(P.steps[c.swap], P.steps[c.swap + 1]);
+    if (c.rows) apply_late_columns(P);
     flatten_plan(P);
   };
   auto smem_of = [&](const Cand& c) { return c.rows ? star_plan_smem_bytes(P, c.rows) : star_smem_bytes(P); };
@@ -1084,7 +1157,8 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
                      ", \"ring_stages\": " + std::to_string(pick.nst) + ", \"tables_staged\": " +
                      (pick.staged ? "true" : "false") + ", \"steps\": \"" + steps + "\", \"grid\": " +
                      std::to_string(grid) + ", \"block\": " + std::to_string(star_block_size()) +
-                     ", \"smem_bytes\": " + std::to_string(smem) + ", \"tuned\": " +
+                     ", \"smem_bytes\": " + std::to_string(smem) + ", \"staged_columns\": " +
+                     std::to_string(P.ncols) + ", \"late_columns\": " + std::to_string(P.nlate) + ", \"tuned\": " +
                      (x->cfg.autotune && cands.size() > 1 ? "true" : "false") + "}";
   }
   x->prof_begin(SVM_K_STAR, &ev);
@@ -1137,7 +1211,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   }
   out->has_bulks = true;
   out->bulk0_rows = out->nrows;
-  x->objects[b.id] = out;
+  x->put_object(b.id, out);
   return SVM_OK;
 }
 
@@ -1592,7 +1666,7 @@ svm_status store_batch_results(Ctx* x, const std::vector<BatchItem>& items, cons
     out->source_rows = out->nrows;
     svm_status st = translate_keys(x, it.b, out);
     if (st) return st;
-    x->objects[it.id] = out;
+    x->put_object(it.id, out);
   }
   return SVM_OK;
 }
@@ -2004,7 +2078,7 @@ svm_status pipeline_footprint(Ctx* x, const svm_pipeline* p, unsigned long long*
     return SVM_OK;
   }
   StarPlan plan;
-  if ((st = plan_star(x, b, src, refs, &plan))) return st;
+  if ((st = plan_star_cached(x, b, src, refs, &plan))) return st;
   const unsigned long long G = plan.P.ngroups;
   // group slots + finalize flags/positions + at most G result rows
   *bytes = 8 * (plan.nmet + 1) * G + 16 * (G + 1) + (4ull * plan.nkeys + 8ull * plan.nmet) * G + 4096;
@@ -2060,7 +2134,7 @@ svm_status run_batch(Ctx* x, int n, const svm_pipeline* p) {
     it.src = src;
     it.b = b;
     it.refs = refs;
-    if ((st = plan_star(x, b, src, refs, &it.plan))) return st;
+    if ((st = plan_star_cached(x, b, src, refs, &it.plan))) return st;
     bool eligible = !it.plan.empty_src && !it.plan.needs_prog;
     for (int m = 0; m < it.plan.nmet; m++) eligible &= it.plan.wide[m] != 0;
     if (!eligible) {
@@ -2157,7 +2231,7 @@ svm_status batch_begin(Ctx* x, int n, const svm_pipeline* p, int want_host, void
       it.src = src;
       it.b = bounds[i];
       it.refs = refs;
-      if ((st = plan_star(x, bounds[i], src, refs, &it.plan))) return fold_fail(x, F, st);
+      if ((st = plan_star_cached(x, bounds[i], src, refs, &it.plan))) return fold_fail(x, F, st);
       bool eligible = !it.plan.empty_src && !it.plan.needs_prog;
       for (int m = 0; m < it.plan.nmet; m++) eligible &= it.plan.wide[m] != 0;
       if (!eligible) {
@@ -2305,6 +2379,15 @@ svm_status batch_wait(Ctx* x, void* fold, void* host, unsigned long long cap, un
     }
   }
   return SVM_OK;
+}
+
+void Ctx::forget_plans(const Object* o) {
+  if (!plan_cache) return;
+  PlanCache* pc = static_cast<PlanCache*>(plan_cache.get());
+  auto f = pc->by_object.find(o);
+  if (f == pc->by_object.end()) return;
+  for (const std::string& k : f->second) pc->plans.erase(k);
+  pc->by_object.erase(f);
 }
 
 void fold_sync(void* fold) {

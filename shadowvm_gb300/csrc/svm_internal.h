@@ -143,7 +143,9 @@ enum AggMode : int { AGG_SCALAR = 0, AGG_DENSE_SMEM = 1, AGG_DENSE_GLOBAL = 2, A
 
 struct StarParams {
   const int32_t* cols[kMaxSteps];   // fact column base pointers (row 0 of the base allocation)
-  int ncols;                        // staged columns
+  int ncols;                        // staged columns (slots 0 .. ncols-1 of cols)
+  int nlate;                        // late columns, slots ncols .. ncols+nlate-1: never staged; a
+                                    // surviving row's value is read from global memory (compiled scan)
   int nstages;                      // ring depth (2..kStages)
   long long row_begin, row_end;     // rows [row_begin, row_end) of the base columns
   int nsteps;
@@ -178,7 +180,8 @@ struct StarParams {
   // words -- the probe words and fact values its keys and metrics read -- are
   // appended to a per-warp buffer and aggregated 32 rows at a time.
   int agg_words;                    // words per buffered row; 0 = aggregate in place
-  int8_t agg_src[kMaxDims + kMaxSteps];  // word k: probe word of dim d (0..3), or fact slot 8 + s
+  int8_t agg_src[kMaxDims + kMaxSteps];  // word k: probe word of dim d (0..3), fact slot 8 + s, or
+                                         // kAggRowWord: the row's index in the base columns
   int8_t agg_step[kMaxDims + kMaxSteps]; // word k: index of the step probing that dim, or fact slot 8 + s
   Extract kx_e[kMaxKeys], xa_e[kMaxMetrics], xb_e[kMaxMetrics];  // the extractors over those words
 };
@@ -302,8 +305,22 @@ struct BatchParams {
 
 // Fills the flattened copies (Step table fields, Extract descriptors) from the
 // structured plan; called on the host once the plan is complete.
+// Aggregation word code of a surviving row's index (late columns gather by it).
+constexpr int kAggRowWord = 16;
+
 inline Extract make_extract(const StarParams& P, Operand o, int32_t adjust) {
   Extract x{};
+  if (o.field < 0 && o.slot >= P.ncols) {
+    // A late column: gathered from global memory by the row word (the
+    // buffered-row extractor makes dim the row word's index).
+    x.dim = -2;
+    x.slot = o.slot;
+    x.shift = 0;
+    x.mask = 0xFFFFFFFFu;
+    x.col = P.cols[o.slot];
+    x.base = adjust;
+    return x;
+  }
   if (o.field < 0) {
     x.dim = -1;
     x.slot = o.slot;
@@ -318,6 +335,42 @@ inline Extract make_extract(const StarParams& P, Operand o, int32_t adjust) {
   x.col = f.col;
   x.base = (int32_t)((uint32_t)(f.col ? 0 : f.min) + (uint32_t)adjust);
   return x;
+}
+
+// Late materialisation (compiled scan only): fact columns that no filter
+// step reads -- only the surviving rows' keys and metrics -- are not
+// staged; they move behind the staged slots (nlate of them) and each
+// survivor's value is read from global memory by its row index.  Call before
+// flatten_plan, on a plan whose columns are all staged.
+inline void apply_late_columns(StarParams& P) {
+  bool by_step[kMaxSteps] = {};
+  for (int k = 0; k < P.nsteps; k++) by_step[P.steps[k].col] = true;
+  if (P.npost > 0 || P.row_end >= (1ll << 32)) return;  // residual programs read staged operands; row words are 32-bit
+  int order[kMaxSteps], remap[kMaxSteps], n = 0;
+  for (int c = 0; c < P.ncols; c++)
+    if (by_step[c]) order[n++] = c;
+  const int staged = n;
+  for (int c = 0; c < P.ncols; c++)
+    if (!by_step[c]) order[n++] = c;
+  if (staged == P.ncols || staged == 0) return;
+  const int32_t* cols[kMaxSteps];
+  for (int i = 0; i < P.ncols; i++) {
+    remap[order[i]] = i;
+    cols[i] = P.cols[order[i]];
+  }
+  for (int i = 0; i < P.ncols; i++) P.cols[i] = cols[i];
+  for (int k = 0; k < P.nsteps; k++) P.steps[k].col = remap[P.steps[k].col];
+  auto fix = [&](Operand& o) {
+    if (o.field < 0) o.slot = (int8_t)remap[o.slot];
+  };
+  for (int q = 0; q < P.nkeys; q++) fix(P.keys[q]);
+  for (int m = 0; m < P.nmetrics; m++) {
+    fix(P.metrics[m].a);
+    if (P.metrics[m].form != MF_OPND) fix(P.metrics[m].b);
+  }
+  for (int i = 0; i < P.nopnd; i++) fix(P.opnds[i]);
+  P.nlate = P.ncols - staged;
+  P.ncols = staged;
 }
 
 inline void flatten_plan(StarParams& P) {
@@ -353,11 +406,11 @@ inline void flatten_plan(StarParams& P) {
   P.agg_words = 0;
   if (prog) return;
   auto word_of = [&](Extract x) {
-    const int8_t code = (int8_t)(x.dim >= 0 ? x.dim : 8 + x.slot);
+    const int8_t code = (int8_t)(x.dim >= 0 ? x.dim : x.dim == -2 ? kAggRowWord : 8 + x.slot);
     int k = 0;
     while (k < P.agg_words && P.agg_src[k] != code) k++;
     if (k == P.agg_words) P.agg_src[P.agg_words++] = code;
-    if (x.dim >= 0)
+    if (x.dim >= 0 || x.dim == -2)
       x.dim = k;
     else
       x.slot = k;

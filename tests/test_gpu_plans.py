@@ -82,3 +82,27 @@ def test_tuned_launch_equals_the_fixed_rule(engine_factory):
         if not tune:
             assert launch["kernel"] == "compiled plan" and launch["rows_per_lane"] == 4
         eng.close()
+
+
+def test_query_mix_compiled_equals_interpreted(engine_factory):
+    """Every query of the batched mix run alone: the compiled kernel (its
+    shapes include a price range in each place the planner puts it) and the
+    interpreted kernel give the same rows, and the mix's shapes all have a
+    compiled kernel."""
+    bw = W.make_batch(60, fact_rows=3_000_000, min_rows=5_000, tuple_per_bulk=1_000_000, n_part=140_000,
+                      n_cust=300_000, n_supp=20_000, qseed=41)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, autotune=False)
+    W.load_batch(eng, bw)
+    compiled = 0
+    for q in bw.queries:
+        eng.pin_launch(0)
+        eng.run(q.pipe)
+        want = eng.result(q.pipe.id, q.key_num)
+        eng.pin_launch(-1)
+        eng.run(q.pipe)
+        got = eng.result(q.pipe.id, q.key_num)
+        compiled += eng.last_launch()["kernel"] == "compiled plan"
+        np.testing.assert_array_equal(got[0], want[0], err_msg=q.pipe.id)
+        np.testing.assert_array_equal(got[1], want[1], err_msg=q.pipe.id)
+    eng.pin_launch()
+    assert compiled == len(bw.queries), compiled
