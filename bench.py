@@ -304,6 +304,9 @@ def ours_arm(args):
     w = W.make(args.config, fact_rows=args.rows)
     rows = w.fact_rows
     eng = Engine(device=local, tuple_per_bulk=w.tuple_per_bulk, join_mode=args.join_mode)
+    if args.pin:
+        r, mb, st, sg = (int(v) for v in args.pin.split(","))
+        eng.pin_launch(r, st, sg, blocks_per_sm=mb)
     W.load_engine(eng, w, row0=rank * rows)
     t_build0 = time.time()
     for p in w.dim_pipelines:
@@ -718,6 +721,9 @@ def main():
     ap.add_argument("--max-fold", type=int, default=1024, help="config 4: most requests in one fold")
     ap.add_argument("--inflight", type=int, default=2, help="config 4: folds begun and not complete, at most")
     ap.add_argument("--loader", action="store_true", help="measure the text Loader instead")
+    ap.add_argument("--pin", default=None,
+                    help="rows_per_lane,blocks_per_sm,ring_stages,tables_staged: pin the scan's launch "
+                         "configuration (svm_pin_launch), e.g. for a profile of one variant")
     ap.add_argument("--join-mode", default="ref_compat", choices=["ref_compat", "exact"])
     args = ap.parse_args()
     if args.warmup < 3:
