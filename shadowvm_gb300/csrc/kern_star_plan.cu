@@ -63,6 +63,9 @@ extern const PlanEntry kPlansMix1[];
 extern const int kPlansMix1Count;
 extern const PlanEntry kPlansMix2[];
 extern const int kPlansMix2Count;
+// The date + part shapes with a presence prefilter (kern_star_plan_mix3.cu).
+extern const PlanEntry kPlansMix3[];
+extern const int kPlansMix3Count;
 
 namespace {
 
@@ -97,6 +100,8 @@ const PlanEntry* find_plan(const StarParams& p, int rows, int minb) {
     if (match(kPlansMix1[i])) return &kPlansMix1[i];
   for (int i = 0; i < kPlansMix2Count; i++)
     if (match(kPlansMix2[i])) return &kPlansMix2[i];
+  for (int i = 0; i < kPlansMix3Count; i++)
+    if (match(kPlansMix3[i])) return &kPlansMix3[i];
   return nullptr;
 }
 

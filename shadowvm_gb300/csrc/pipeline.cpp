@@ -934,6 +934,69 @@ svm_status plan_star_cached(Ctx* x, const Bound& b, const ObjectPtr& src, const 
   return SVM_OK;
 }
 
+// Presence prefilter (single-query scans).  A selective join whose dense
+// table carries a payload and is too big to stage -- the part table of the
+// date + part query: 400 K one-byte entries probed in L2 by every fact row,
+// 4 % of them present -- gets a second, payload-less table over the same
+// keys (one bit a key, the same rows inserted, so REF_COMPAT drops the same
+// keys): its probe takes the payload probe's place, and the payload probe
+// moves behind every other step, where only surviving rows reach it.  The
+// bit table is small enough to stay in L1 or in shared memory.
+svm_status add_presence_prefilters(Ctx* x, const Bound& b, const std::vector<ObjectPtr>& refs, StarPlan* plan) {
+  StarParams& P = plan->P;
+  if (plan->empty_src || plan->needs_prog) return SVM_OK;
+  const int nref = (int)refs.size();
+  std::vector<int> dim_obj;  // dim index -> joined object (1..nref), as plan_star numbers them
+  std::vector<int> key_col;
+  for (int k = 1; k <= nref; k++)
+    for (size_t j = 0; j < b.join_rkey.size(); j++)
+      if (b.join_rkey[j].obj == k) {
+        dim_obj.push_back(k);
+        key_col.push_back(b.join_rkey[j].col);
+      }
+  if ((int)dim_obj.size() != P.ndims) return SVM_OK;
+  const int ndims0 = P.ndims;
+  bool done[kMaxDims] = {};
+  for (int s = 0; s < P.nsteps && P.ndims < kMaxDims && P.nsteps < kMaxSteps; s++) {
+    const Step st = P.steps[s];
+    if (st.kind != STEP_PROBE || st.dim >= ndims0 || done[st.dim]) continue;
+    const DimDesc& D = P.dims[st.dim];
+    if (D.layout != LAYOUT_DENSE || D.smem_word_off >= 0 || D.entry_bits < 2) continue;
+    const DimTablePtr& T = plan->dim_tables[st.dim];
+    const ObjectPtr& o = refs[dim_obj[st.dim] - 1];
+    const double pass = (double)T->live / (double)std::max<unsigned long long>(1, o->source_rows);
+    if (pass > 0.1 || (unsigned long long)D.span / 8 > (unsigned long long)kSmemTableBytes) continue;
+    DimTablePtr pres;
+    svm_status r = build_dim(x, o, key_col[st.dim], {}, &pres);
+    if (r) return r;
+    if (pres->desc.layout != LAYOUT_DENSE || pres->desc.entry_bits != 1) continue;
+    done[st.dim] = true;
+    const int nd = P.ndims++;
+    P.dims[nd] = pres->desc;
+    P.dims[nd].smem_word_off = -1;
+    const int words = (int)((pres->desc.table_words + 3) & ~3u);
+    if (P.smem_table_words + words <= kSmemTableBytes / 4) {  // staged when it fits beside the others
+      P.dims[nd].smem_word_off = P.smem_table_words;
+      P.smem_table_words += words;
+    }
+    plan->dim_tables.push_back(pres);
+    // the bit probe (with any folded key range) in place of the payload probe,
+    // which moves behind every other step
+    Step bit = st;
+    bit.dim = nd;
+    Step payload = st;
+    payload.lo = INT_MIN;
+    payload.hi = INT_MAX;
+    for (int k = s; k + 1 < P.nsteps; k++) P.steps[k] = P.steps[k + 1];
+    P.steps[P.nsteps - 1] = payload;
+    for (int k = P.nsteps; k > s; k--) P.steps[k] = P.steps[k - 1];
+    P.steps[s] = bit;
+    P.nsteps++;
+  }
+  flatten_plan(P);
+  return SVM_OK;
+}
+
 // The shape a star launch is tuned for: columns, steps (kind, table layout,
 // placement, entry width), dimensions, aggregation, and the orders of
 // magnitude of the group count and the rows scanned.
@@ -986,6 +1049,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   StarPlan plan;
   svm_status st = plan_star_cached(x, b, src, refs, &plan);
   if (st) return st;
+  if ((st = add_presence_prefilters(x, b, refs, &plan))) return st;
   const std::vector<int>& out_types = plan.out_types;
   const int nkeys = plan.nkeys, nmet = plan.nmet;
   const int* wide = plan.wide;
