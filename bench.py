@@ -579,9 +579,15 @@ def served_arm(args):
         eng.run(p)
     for _ in range(args.warmup):  # dimension tables, merged tables, device pool
         eng.run_batch([q.pipe for q in bw.queries])
+    alone = {}
     for q in bw.queries:
         eng.run(q.pipe)
+        alone[q.pipe.id] = eng.result(q.pipe.id, q.key_num)
     pick = np.random.default_rng(4321).integers(0, len(bw.queries), size=10_000_000)
+
+    def check(i, res):  # every served result against its query run alone
+        want = alone[bw.queries[pick[i]].pipe.id]
+        return bool(np.array_equal(res[0], want[0]) and np.array_equal(res[1], want[1]))
 
     def make_pipe(i):
         q = bw.queries[pick[i]]
@@ -597,7 +603,7 @@ def served_arm(args):
             eng.profile_reset()
             with serving.BatchLoop(eng, budget_bytes=150 * 10**9, serial=(mode == "serial"), fetch=True,
                                    drop_results=True, max_fold=args.max_fold, inflight=args.inflight) as loop:
-                r = serving.poisson_run(loop, make_pipe, rate, args.serve_seconds, seed=int(rate))
+                r = serving.poisson_run(loop, make_pipe, rate, args.serve_seconds, seed=int(rate), check=check)
             r["device_s"] = {name: eng.profile_read(k)[1] / 1e3 for name, k in
                              (("batch", capi.K_BATCH), ("star", capi.K_STAR), ("finalize", capi.K_FINALIZE))}
             eng.profile(False)
@@ -625,7 +631,9 @@ def served_arm(args):
                                    "batched_p99_ms": top_b["latency_ms"]["p99"],
                                    "serial_p99_ms": top_s["latency_ms"]["p99"]},
                       "max_sustained_qps": {"batched": sb["achieved_qps"] if sb else None,
-                                            "serial": ss["achieved_qps"] if ss else None}},
+                                            "serial": ss["achieved_qps"] if ss else None},
+                      "results_checked": sum(p["checked"] for m in points.values() for p in m),
+                      "results_equal_to_alone": all(p["mismatched"] == 0 for m in points.values() for p in m)},
            "clocks": clk,
            "e2e": {"value": top_b["achieved_qps"], "unit": "queries/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": None, "note": "every request's result is copied to the host"}}

@@ -318,10 +318,13 @@ def split_result(cols, key_num: int):
     return keys, sums
 
 
-def poisson_run(loop: BatchLoop, make_pipe, rate: float, seconds: float, seed: int = 0, tick: float = 0.0005):
+def poisson_run(loop: BatchLoop, make_pipe, rate: float, seconds: float, seed: int = 0, tick: float = 0.0005,
+                check=None):
     """Submits a seeded Poisson stream of `rate` requests/s for `seconds`
     (make_pipe(i) -> (PipelineInfo, key_num) builds request i) and waits for
-    all of them.  Returns throughput and latency statistics."""
+    all of them.  Returns throughput and latency statistics; with `check`
+    (check(i, result) -> bool, on the fetched results) also how many
+    results it accepted and rejected."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate, size=int(rate * seconds * 1.2) + 16)
     arrivals = np.cumsum(gaps)
@@ -343,11 +346,16 @@ def poisson_run(loop: BatchLoop, make_pipe, rate: float, seconds: float, seed: i
         if i < n:
             time.sleep(max(0.0, min(tick, arrivals[i] - (time.perf_counter() - t0))))
     errors = 0
-    for f in futures:
+    checked = mismatched = 0
+    for i, f in enumerate(futures):
         try:
-            f.result()
+            res = f.result()
         except Exception:
             errors += 1
+            continue
+        if check is not None:
+            checked += 1
+            mismatched += 0 if check(i, res) else 1
     reqs = [f.request for f in futures]
     lat = np.array([(r.t_done - r.t_arrival) * 1e3 for r in reqs]) if reqs else np.zeros(1)
     t_end = max(r.t_done for r in reqs) if reqs else t0
@@ -358,4 +366,5 @@ def poisson_run(loop: BatchLoop, make_pipe, rate: float, seconds: float, seed: i
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "p999": float(np.percentile(lat, 99.9)), "max": float(lat.max())},
             "folds": len(per_fold), "mean_fold": float(np.mean(list(per_fold.values()))) if per_fold else 0.0,
-            "host_s": dict(loop.phase_s, submit=submit_s)}
+            "host_s": dict(loop.phase_s, submit=submit_s),
+            "checked": checked, "mismatched": mismatched}
