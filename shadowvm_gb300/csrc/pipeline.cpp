@@ -1421,8 +1421,9 @@ struct BatchItem {
 };
 
 // Cost model of a fold, in picoseconds, measured on GB300 with the 256-query
-// star-schema mix over a 600 M-row table: one query alone costs about 4.6 ps
-// per row it reads plus ~30 us of launch, finalize and result handling; the
+// star-schema mix over a 600 M-row table: one query alone costs about 3.5 ps
+// per row it reads (the compiled scans: 90 ms of kernels for the mix's 25.5 G
+// query-rows) plus ~90 us of launch, finalize and result handling; the
 // batched launch costs about 46 ps per row of the union of the queries'
 // ranges (the shared scan, merged-table lookups, bitmaps and per-tile
 // bookkeeping: 27.6 ms for the 600 M-row union with the query work removed)
@@ -1435,7 +1436,7 @@ bool batch_is_cheaper(const std::vector<BatchItem>& items) {
     const long long b = it.plan.P.row_begin, e = it.plan.empty_filter ? b : it.plan.P.row_end;
     iv.push_back({b, e});
     rows += (double)(e - b);
-    single += 4.6 * (double)(e - b) + 30e6;
+    single += 3.5 * (double)(e - b) + 90e6;
   }
   std::sort(iv.begin(), iv.end());
   double uni = 0;
