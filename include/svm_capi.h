@@ -320,10 +320,19 @@ svm_status svm_scan_aggregate_noalloc(svm_ctx* ctx, const svm_noalloc_scan* q, i
  * 1024 threads a block, com/cpp/com.cu:19-20). */
 svm_status svm_pin_launch(svm_ctx* ctx, int rows_per_lane, int blocks_per_sm, int ring_stages, int tables_staged);
 
+/* The same for the merged batch kernel of svm_run_batch / svm_batch_begin:
+ * consumer_warps 0 (any), 28 or 24 of its 32 warps (the others look rows
+ * up in the merged tables and issue the bulk copies), ring_stages 0 (any)
+ * or 2..4 (at most the depth at which every descriptor of a launch still
+ * fits).  With autotuning, the first launch of each batch shape times the
+ * candidates left and keeps the fastest.  No counterpart in the reference. */
+svm_status svm_pin_batch_launch(svm_ctx* ctx, int consumer_warps, int ring_stages);
+
 /* The launch configuration of the context's last fused scan (the kernel
  * compiled for the plan's shape or the interpreted one, rows per consumer
  * lane, ring stages, table placement, the steps in order, grid and shared
- * memory), as a JSON object in `buf` (cut to cap - 1 bytes, NUL-terminated;
+ * memory) or merged batch launch (warp split, ring stages, queries per
+ * launch), as a JSON object in `buf` (cut to cap - 1 bytes, NUL-terminated;
  * empty before the first scan).  No counterpart in the reference. */
 svm_status svm_last_launch(svm_ctx* ctx, char* buf, unsigned long long cap);
 

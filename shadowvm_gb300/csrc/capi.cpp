@@ -802,6 +802,18 @@ svm_status svm_pin_launch(svm_ctx* c, int rows_per_lane, int blocks_per_sm, int 
   return SVM_OK;
 }
 
+svm_status svm_pin_batch_launch(svm_ctx* c, int consumer_warps, int ring_stages) {
+  if (!c) return SVM_E_INVALID_ARG;
+  if (!(consumer_warps == 0 || consumer_warps == 24 || consumer_warps == 28) ||
+      !(ring_stages == 0 || (ring_stages >= 2 && ring_stages <= svm::kStages)))
+    return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  x->pin_batch_cw = consumer_warps;
+  x->pin_batch_stages = ring_stages;
+  return SVM_OK;
+}
+
 svm_status svm_last_launch(svm_ctx* c, char* buf, unsigned long long cap) {
   if (!c || !buf || cap == 0) return SVM_E_INVALID_ARG;
   Ctx* x = C(c);

@@ -181,6 +181,11 @@ struct Ctx {
   // staged (-1: any).  A pin narrows the candidates; the rule or
   // the tuner picks among those left.
   int pin_rows = -1, pin_minb = 0, pin_stages = 0, pin_staged = -1;
+  // Pinned merged-batch launch choices (svm_pin_batch_launch): consumer warps
+  // (0: any, 28 or 24) and ring stages (0: any).
+  int pin_batch_cw = 0, pin_batch_stages = 0;
+  // Tuned merged-batch launches: batch shape -> (consumer warps, ring stages).
+  std::map<std::string, std::pair<int, int>> batch_tune;
   // Planned fact pipelines by content and the versions of the objects they
   // read (pipeline.cpp); forget_plans drops the plans that read `o`.
   std::shared_ptr<void> plan_cache;

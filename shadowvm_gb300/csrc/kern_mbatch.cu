@@ -22,14 +22,15 @@
 namespace svm {
 namespace {
 
-constexpr int kFillWarps = 4;  // warp kMBatchWarps also issues the bulk copies
-constexpr int kMBThreads = (kMBatchWarps + kFillWarps) * 32;
-constexpr int kMBConsumers = kMBatchWarps * 32;
-constexpr int kFillRows = kTileRows / kFillWarps;
+// The block is 32 warps: kCW consumer warps and 32 - kCW fill warps (the
+// first fill warp also issues the bulk copies); the split is a template
+// parameter the launch tuner chooses (28 + 4 or 24 + 8).
+constexpr int kMBThreads = 1024;
 constexpr uint32_t kPolls = 1u << 22;
 
+template <int kCW>
 __device__ __forceinline__ void consumer_bar() {
-  asm volatile("bar.sync 1, %0;" ::"n"(kMBConsumers) : "memory");
+  asm volatile("bar.sync 1, %0;" ::"n"(kCW * 32) : "memory");
 }
 
 __device__ __forceinline__ uint32_t lane_lt() {
@@ -280,7 +281,12 @@ __device__ __forceinline__ uint32_t tile_queries(const long long* qlo, const lon
   return __reduce_or_sync(0xffffffffu, need);
 }
 
+template <int kCW>
 __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_constant__ BatchParams B) {
+  constexpr int kMBatchWarps = kCW;              // consumer warps
+  constexpr int kFillWarps = 32 - kCW;           // fill warps (the first also issues the bulk copies)
+  constexpr int kFillRows = kTileRows / kFillWarps;
+  static_assert(kTileRows % kFillWarps == 0, "fill warps split a tile evenly");
   extern __shared__ __align__(128) uint8_t dyn[];
   __shared__ uint64_t full[kStages], empty[kStages];
   __shared__ uint64_t fill_full[2], fill_empty[2];
@@ -429,7 +435,7 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
       s_na = t0 >= 0 ? s_list_na[b] : 0;
       s_need = t0 >= 0 ? s_list_need[b] : 0u;
     }
-    consumer_bar();
+    consumer_bar<kCW>();
     const long long t = s_tile;
     if (t < 0) {
       if (t == -2 && tid == 0) raise_error(B.error, DERR_TIMEOUT);
@@ -459,7 +465,7 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
       const int t0 = B.gtab0[g];
       if (lane < B.gtab0[g + 1] - t0) bm[(t0 + lane) * kBmStride + chunk] = present;
     }
-    consumer_bar();
+    consumer_bar<kCW>();
     // Queries, claimed one at a time.
     for (;;) {
       int k = 0;
@@ -471,7 +477,7 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
       const long long hi = qhi[q] < tile_end ? qhi[q] - tile_start : kTileRows;
       mquery_tile(sq[q], B, stage, mw, bm, (int)lo, (int)hi, lane, lt, aggring + warp * kAggRing);
     }
-    consumer_bar();
+    consumer_bar<kCW>();
     if (tid == 0) {
       mbar_arrive(&empty[s]);
       mbar_arrive(&fill_empty[b]);
@@ -525,22 +531,31 @@ cudaError_t launch_merge_build(const MergeBuild& m, uint32_t* out, cudaStream_t 
   return cudaGetLastError();
 }
 
+namespace {
+int cwarps_of(const BatchParams& b) { return b.cwarps == 24 ? 24 : 28; }
+const void* mbatch_fn(const BatchParams& b) {
+  return cwarps_of(b) == 24 ? reinterpret_cast<const void*>(&mbatch_kernel<24>)
+                            : reinterpret_cast<const void*>(&mbatch_kernel<28>);
+}
+}  // namespace
+
 size_t mbatch_smem_bytes(const BatchParams& b) {
   return (size_t)b.nstages * b.ncols * kTileRows * 4 + 2 * (size_t)b.nmwords * kSlots * 4 +
          (size_t)kMaxMergedTables * kBmStride * 4 + (size_t)b.nqueries * (sizeof(MQuery) + 8 + 8 + 4 + 4) +
-         (size_t)kMBatchWarps * kAggRing * 2 + 16;
+         (size_t)cwarps_of(b) * kAggRing * 2 + 16;
 }
 
 int mbatch_grid_size(const BatchParams& b, size_t smem) {
-  allow_dynamic_smem(reinterpret_cast<const void*>(&mbatch_kernel), 226 * 1024);
+  const void* fn = mbatch_fn(b);
+  allow_dynamic_smem(fn, 226 * 1024);
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mbatch_kernel, kMBThreads, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kMBThreads, smem);
   return num_sms() * per_sm;
 }
 
 void mbatch_attributes(int* regs, int* max_threads, size_t* static_smem) {
   cudaFuncAttributes a{};
-  cudaFuncGetAttributes(&a, mbatch_kernel);
+  cudaFuncGetAttributes(&a, reinterpret_cast<const void*>(&mbatch_kernel<28>));
   *regs = a.numRegs;
   *max_threads = a.maxThreadsPerBlock;
   *static_smem = a.sharedSizeBytes;
@@ -548,8 +563,8 @@ void mbatch_attributes(int* regs, int* max_threads, size_t* static_smem) {
 
 cudaError_t launch_mbatch(const BatchParams& b, int grid, size_t smem, cudaStream_t s) {
   note_launch();
-  mbatch_kernel<<<grid, kMBThreads, smem, s>>>(b);
-  return cudaGetLastError();
+  void* args[] = {const_cast<BatchParams*>(&b)};
+  return cudaLaunchKernel(mbatch_fn(b), dim3(grid), dim3(kMBThreads), args, smem, s);
 }
 
 }  // namespace svm

@@ -2050,8 +2050,73 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items, FoldPart* async_par
       for (size_t g = 0; g < mp.gtab0.size(); g++) B.gtab0[g] = mp.gtab0[g];
       for (size_t c = 0; c < gcols.size(); c++) B.gcol[c] = gcols[c];
       B.nstages = mst;
+      B.cwarps = kMBatchWarps;
+      // Launch configuration of the merged kernel: the consumer / fill warp
+      // split (28 + 4 or 24 + 8) and the ring depth (at most the rule's,
+      // which fits every descriptor of the launch).  The rule: 28 + 4, the
+      // deepest ring.  With autotuning, the first launch of a batch shape
+      // times every candidate on the batch itself (slots and tile counters
+      // zeroed before each and again after), and the fastest is kept.
+      std::vector<std::pair<int, int>> cands;  // (consumer warps, ring stages)
+      for (int cw : {28, 24})
+        for (int nst = mst; nst >= 2; nst--)
+          if ((!x->pin_batch_cw || cw == x->pin_batch_cw) && (!x->pin_batch_stages || nst == x->pin_batch_stages))
+            cands.push_back({cw, nst});
+      if (cands.empty()) return x->fail(SVM_E_UNSUPPORTED, "no batch launch configuration fits the pinned choices");
+      std::pair<int, int> pick = cands[0];
+      bool tuned = false;
+      const std::string key = "q" + std::to_string(ceil_log2((unsigned long long)qn + 1)) + ":c" +
+                              std::to_string(B.ncols) + ":w" + std::to_string(B.nmwords) + ":g" +
+                              std::to_string(B.nprobe) + ":s" + std::to_string(mst) + ":pin" +
+                              std::to_string(x->pin_batch_cw) + "," + std::to_string(x->pin_batch_stages);
+      if (x->cfg.autotune && cands.size() > 1) {
+        auto hit = x->batch_tune.find(key);
+        if (hit != x->batch_tune.end()) {
+          pick = hit->second;
+        } else {
+          cudaEvent_t t0, t1;
+          cudaEventCreate(&t0);
+          cudaEventCreate(&t1);
+          float best = 0.f;
+          for (const auto& c : cands) {
+            B.cwarps = c.first;
+            B.nstages = c.second;
+            const size_t sm = mbatch_smem_bytes(B);
+            const int g = mbatch_grid_size(B, sm);
+            if (g <= 0) continue;
+            if (!e) e = cudaMemsetAsync(slots, 0, 8 * slot_words, x->stream);
+            if (!e) e = cudaMemsetAsync(ctr, 0, 8 * (nlaunch + 1), x->stream);
+            if (!e) e = cudaEventRecord(t0, x->stream);
+            if (!e) e = launch_mbatch(B, g, sm, x->stream);
+            if (!e) e = cudaEventRecord(t1, x->stream);
+            if (!e) e = cudaEventSynchronize(t1);
+            float ms = 0.f;
+            if (!e) e = cudaEventElapsedTime(&ms, t0, t1);
+            if (e) break;
+            if (best == 0.f || ms < best) {
+              best = ms;
+              pick = c;
+            }
+          }
+          cudaEventDestroy(t0);
+          cudaEventDestroy(t1);
+          if (!e) e = cudaMemsetAsync(slots, 0, 8 * slot_words, x->stream);
+          if (!e) e = cudaMemsetAsync(ctr, 0, 8 * (nlaunch + 1), x->stream);
+          if (e) return x->cuda_fail(e, "batch kernel tuning");
+          x->batch_tune[key] = pick;
+        }
+        tuned = true;
+      }
+      B.cwarps = pick.first;
+      B.nstages = pick.second;
       const size_t smem = mbatch_smem_bytes(B);
       const int grid = mbatch_grid_size(B, smem);
+      x->last_launch = "{\"kernel\": \"batch\", \"consumer_warps\": " + std::to_string(pick.first) +
+                       ", \"fill_warps\": " + std::to_string(32 - pick.first) + ", \"ring_stages\": " +
+                       std::to_string(pick.second) + ", \"queries_per_launch\": " + std::to_string(per_launch) +
+                       ", \"merged_launches\": " + std::to_string(nlaunch) + ", \"queries\": " +
+                       std::to_string(nq) + ", \"grid\": " + std::to_string(grid) + ", \"smem_bytes\": " +
+                       std::to_string(smem) + ", \"tuned\": " + (tuned ? "true" : "false") + "}";
       if (grid <= 0) {
         int regs = 0, maxt = 0;
         size_t ss = 0;

@@ -200,7 +200,7 @@ constexpr int kMaxBatchCols = 12;
 // group then serves every query of the batch that probes any of those tables.
 constexpr int kMaxProbeGroups = 8;
 constexpr int kMaxMergedWords = 16;   // merged words per row over all groups
-constexpr int kMBatchWarps = 28;      // consumer warps of the merged batch kernel
+constexpr int kMBatchWarps = 28;      // consumer warps of the merged batch kernel (the rule's split)
 
 struct ProbeGroup {
   int col;                  // union fact column slot of the key
@@ -301,6 +301,7 @@ struct BatchParams {
   const MQuery* mq;                 // merged kernel: descriptors (nqueries)
   int gtab0[kMaxProbeGroups + 1];   // group g's tables are slots [gtab0[g], gtab0[g + 1]), in present-bit order
   const int32_t* gcol[kMaxGatherCols];  // row-index payload columns (MExtract::sg high bits)
+  int cwarps;                       // merged kernel: consumer warps of the 32 (28 or 24; 0 = 28)
 };
 
 // Fills the flattened copies (Step table fields, Extract descriptors) from the

@@ -244,6 +244,11 @@ class Engine:
         the defaults lift every pin."""
         self._check(self.lib.svm_pin_launch(self.h, rows_per_lane, blocks_per_sm, ring_stages, tables_staged))
 
+    def pin_batch_launch(self, consumer_warps: int = 0, ring_stages: int = 0):
+        """Narrows the merged batch kernel's launch configurations
+        (svm_pin_batch_launch); the defaults lift every pin."""
+        self._check(self.lib.svm_pin_batch_launch(self.h, consumer_warps, ring_stages))
+
     def last_launch(self) -> dict:
         """The last fused scan's launch configuration (svm_last_launch)."""
         import json

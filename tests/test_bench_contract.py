@@ -13,12 +13,16 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def test_star_kernel_traffic_is_committed():
     tr = bench.committed_traffic(2)
     assert tr is not None
-    # five int32 columns read once: 20 B per fact row, a little above for the
-    # probe tables and the group slots
-    assert 20.0 <= tr["dram_bytes_per_row"] < 20.5
-    assert "star_kernel_config2.md" in tr["source"]
+    # three int32 columns streamed (12 B per fact row) and the two late metric
+    # columns gathered at the surviving rows' sectors: below the 20 B the five
+    # columns would take
+    assert 12.0 < tr["dram_bytes_per_row"] < 20.0
+    assert "star_plan_kernel_config2.md" in tr["source"]
     # the String-dimension query runs the same kernel over the same fact columns
     assert bench.committed_traffic(5) == tr
+    # configs 0 and 1 have captures of their own
+    assert 8.0 < bench.committed_traffic(1)["dram_bytes_per_row"] < 12.0
+    assert 12.0 < bench.committed_traffic(0)["dram_bytes_per_row"] < 16.0
 
 
 def test_batch_kernel_traffic_is_committed():

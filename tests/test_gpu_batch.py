@@ -208,3 +208,34 @@ def test_batch_policy(engine_factory, policy):
     for i in one:
         np.testing.assert_array_equal(many[i][0], one[i][0])
         np.testing.assert_array_equal(many[i][1], one[i][1])
+
+
+def test_batch_launch_variants_equal_single_launches(engine_factory):
+    """The merged kernel's launch variants the tuner chooses from -- 28 or 24
+    consumer warps of 32, and the ring depth -- give each query the rows it
+    has alone; the tuned launch too, and it is reported."""
+    bw = W.make_batch(48, qseed=43, **SMALL)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, batch_policy="always", autotune=False)
+    W.load_batch(eng, bw)
+    one = singles(eng, bw)
+    seen = set()
+    for cw in (28, 24):
+        for st in (2, 3):
+            eng.pin_batch_launch(cw, st)
+            got = batched(eng, bw)
+            launch = eng.last_launch()
+            assert launch["kernel"] == "batch" and launch["consumer_warps"] == cw, launch
+            seen.add((cw, launch["ring_stages"]))
+            for i in one:
+                np.testing.assert_array_equal(got[i][0], one[i][0], err_msg=f"{cw} warps, {st} stages, query {i}")
+                np.testing.assert_array_equal(got[i][1], one[i][1], err_msg=f"{cw} warps, {st} stages, query {i}")
+    eng.pin_batch_launch()
+    assert len(seen) >= 3
+    tuned = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, batch_policy="always", autotune=True)
+    W.load_batch(tuned, bw)
+    for _ in range(2):  # tuned on the first batch, cached for the second
+        got = batched(tuned, bw)
+        for i in one:
+            np.testing.assert_array_equal(got[i][0], one[i][0])
+            np.testing.assert_array_equal(got[i][1], one[i][1])
+    assert tuned.last_launch()["tuned"] is True

@@ -106,3 +106,43 @@ def test_query_mix_compiled_equals_interpreted(engine_factory):
         np.testing.assert_array_equal(got[1], want[1], err_msg=q.pipe.id)
     eng.pin_launch()
     assert compiled == len(bw.queries), compiled
+
+
+def test_plan_cache_follows_replaced_objects(engine_factory):
+    """Plans are cached by pipeline content and the versions and row ranges
+    of the objects they read: replacing a dimension, rerunning its pipeline
+    and viewing another row range each give the result a fresh plan gives."""
+    import oracle
+    case = GOLDEN["c2_small"]
+    w = W.make(case["config"], **case["kwargs"])
+    eng = engine_factory(tuple_per_bulk=w.tuple_per_bulk, join_mode="exact")
+    W.load_engine(eng, w)
+    k1, s1 = W.run_engine(eng, w)
+    ek, es = oracle.exact_workload(w)
+    np.testing.assert_array_equal(k1, ek)
+    np.testing.assert_array_equal(s1, es)
+    # the same pipeline text again: the cached plan, the same rows
+    eng.run(w.query)
+    k2, s2 = eng.result(w.query.id, w.key_num)
+    np.testing.assert_array_equal(s2, s1)
+    # a different customer table under the same id: every customer's nation shifts by one within its region
+    cust = [c.copy() for c in w.dims["customer"]]
+    cust[2] = (cust[3] * 5 + (cust[2] - cust[3] * 5 + 1) % 5).astype(np.int32)
+    w.dims["customer"] = cust
+    eng.put("customer", cust)
+    k3, s3 = W.run_engine(eng, w)
+    ek3, es3 = oracle.exact_workload(w)
+    np.testing.assert_array_equal(k3, ek3)
+    np.testing.assert_array_equal(s3, es3)
+    assert not np.array_equal(k3, k1) or not np.array_equal(s3, s1)
+    # a view of a row range: its own plan
+    eng.view("lo_part", "lineorder", 1000, 50_000)
+    q = W.fact_pipeline("q2_part", "lo_part", w.fact_schema(), list(w.query.pre_pipeline_id[1:]),
+                        [("$(0.0)", "$(1.0)"), ("$(0.5)", "$(2.0)"), ("$(0.6)", "$(3.0)")],
+                        "$(2.1),$(3.1),$(1.1)", "$(0.7)-$(0.8)")
+    eng.run(q)
+    kp, sp = eng.result("q2_part", 3)
+    fact = [c[1000:51_000] for c in w.fact_host(0, w.fact_rows)]
+    ekp, esp = oracle.exact_workload(w, fact)
+    np.testing.assert_array_equal(kp, ekp)
+    np.testing.assert_array_equal(sp, esp)
