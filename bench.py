@@ -274,6 +274,7 @@ def batched_measure(eng, bw, steps: int, warmup: int):
         batch_walls.append(time.perf_counter() - t0)
     n_b, b_ms = eng.profile_read(capi.K_BATCH)
     eng.profile(False)
+    batch_launch = eng.last_launch()
     serial_s, batch_s = statistics.median(serial_walls), statistics.median(batch_walls)
     lat = np.array(lat)
     bl = np.array(batch_walls) * 1e3
@@ -286,7 +287,7 @@ def batched_measure(eng, bw, steps: int, warmup: int):
             "device_ms": {"batch_kernel": b_ms / max(n_b, 1), "serial_star_kernels": star_ms / max(1, n_star) * nq},
             "query_rows_total": int(sum(q.nrows for q in bw.queries)),
             "shapes": {str(k): sum(q.shape == k for q in bw.queries) for k in range(3)},
-            "bit_exact_vs_one_query_per_launch": bool(exact)}
+            "bit_exact_vs_one_query_per_launch": bool(exact), "launch": batch_launch}
 
 
 def ours_arm(args):
