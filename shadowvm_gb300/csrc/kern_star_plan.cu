@@ -27,9 +27,9 @@
 // the compiler gets) set how many warps wait on those loads at once.  Lane L
 // owns rows 4L..4L+3 of each 128-row slice of its warp's rows, so every
 // column read is one conflict-free 16-byte shared-memory load per slice.
-// When no probed table's entry is wider than 16 bits, the entries kept for
-// the aggregation are stored as 16-bit words, halving that part of the
-// block's shared memory.
+// The entries kept for the aggregation are stored in the narrowest of 8-,
+// 16- and 32-bit words that holds every probed table's entries; with 8-bit
+// words the four-dimension star join's block fits three to an SM.
 #include "kern_star_plan.cuh"
 
 namespace svm {
@@ -124,11 +124,11 @@ bool star_plan_available(const StarParams& p, int rows_per_lane, int min_blocks)
 
 size_t star_plan_smem_bytes(const StarParams& p, int rows_per_lane) {
   const size_t tr = (size_t)kConsumerWarps * plan_warp_rows(rows_per_lane);
-  bool narrow = true;
+  int bits = 0;
   for (int k = 0; k < p.nsteps; k++)
-    if (p.steps[k].kind == STEP_PROBE && p.steps[k].entry_bits > 16) narrow = false;
+    if (p.steps[k].kind == STEP_PROBE && p.steps[k].entry_bits > bits) bits = p.steps[k].entry_bits;
   size_t b = (size_t)p.nstages * p.ncols * tr * 4;
-  b += plan_list_bytes(p.ndims, rows_per_lane, narrow) * kConsumerWarps;
+  b += plan_list_bytes(p.ndims, rows_per_lane, plan_entry_bytes(bits)) * kConsumerWarps;
   b += (size_t)((p.smem_table_words + 3) & ~3) * 4;
   if (p.agg == AGG_DENSE_SMEM) b += (size_t)p.ngroups * (8 * p.nmetrics + 4);
   b = (b + 15) & ~size_t(15);

@@ -30,10 +30,16 @@ __host__ __device__ constexpr int plan_warp_rows(int rows_per_lane) { return 32 
 
 // One consumer warp's survivor list: row offsets within the warp's rows and,
 // per joined dimension, each row's table entry (indexed by row offset), in
-// 16-bit words when every entry fits them.
-__host__ __device__ inline size_t plan_list_bytes(int ndims, int rows_per_lane, bool narrow) {
+// 8- or 16-bit words when every entry fits them (entry_bytes 1, 2 or 4).
+__host__ __device__ inline size_t plan_list_bytes(int ndims, int rows_per_lane, int entry_bytes) {
   const size_t wr = (size_t)plan_warp_rows(rows_per_lane);
-  return ((size_t)(ndims > 0 ? ndims : 1) * wr * (narrow ? 2 : 4) + wr * 2 + 15) & ~size_t(15);
+  return ((size_t)(ndims > 0 ? ndims : 1) * wr * entry_bytes + wr * 2 + 15) & ~size_t(15);
+}
+
+// The bytes a kept entry takes: the narrowest of 1, 2 and 4 that holds every
+// probe step's entries (the host side is star_plan_smem_bytes).
+__host__ __device__ constexpr int plan_entry_bytes(int max_entry_bits) {
+  return max_entry_bits <= 8 ? 1 : max_entry_bits <= 16 ? 2 : 4;
 }
 
 template <int kR, typename PwT>
@@ -43,11 +49,15 @@ struct PlanList {
   __device__ __forceinline__ PwT* pw(int d) const { return pwb + d * plan_warp_rows(kR); }
 };
 
-// Whether every probe step's entries fit 16 bits.
+// The kept-entry word of a shape: the narrowest that holds every probe
+// step's entries.
 template <int A, int B, int C, int D>
-struct PlanNarrow {
+struct PlanEntryWord {
   static constexpr int bits(int code) { return ((code & 3) >= SC_SMEM) ? (1 << ((code >> 2) & 7)) : 0; }
-  static constexpr bool value = bits(A) <= 16 && bits(B) <= 16 && bits(C) <= 16 && bits(D) <= 16;
+  static constexpr int max2(int a, int b) { return a > b ? a : b; }
+  static constexpr int bytes = plan_entry_bytes(max2(max2(bits(A), bits(B)), max2(bits(C), bits(D))));
+  using type = typename std::conditional<bytes == 1, uint8_t,
+                                         typename std::conditional<bytes == 2, uint16_t, uint32_t>::type>::type;
 };
 
 template <typename PwT, int kR>
@@ -61,6 +71,15 @@ template <>
 __device__ __forceinline__ void store_entries<uint32_t, 8>(uint32_t* out, int lane, const uint32_t (&e)[8]) {
   *reinterpret_cast<uint4*>(out + 4 * lane) = make_uint4(e[0], e[1], e[2], e[3]);
   *reinterpret_cast<uint4*>(out + 128 + 4 * lane) = make_uint4(e[4], e[5], e[6], e[7]);
+}
+template <>
+__device__ __forceinline__ void store_entries<uint8_t, 4>(uint8_t* out, int lane, const uint32_t (&e)[4]) {
+  *reinterpret_cast<uint32_t*>(out + 4 * lane) = e[0] | e[1] << 8 | e[2] << 16 | e[3] << 24;
+}
+template <>
+__device__ __forceinline__ void store_entries<uint8_t, 8>(uint8_t* out, int lane, const uint32_t (&e)[8]) {
+  *reinterpret_cast<uint32_t*>(out + 4 * lane) = e[0] | e[1] << 8 | e[2] << 16 | e[3] << 24;
+  *reinterpret_cast<uint32_t*>(out + 128 + 4 * lane) = e[4] | e[5] << 8 | e[6] << 16 | e[7] << 24;
 }
 template <>
 __device__ __forceinline__ void store_entries<uint16_t, 4>(uint16_t* out, int lane, const uint32_t (&e)[4]) {
@@ -148,8 +167,7 @@ __device__ __forceinline__ void plan_step_if(const Step& st, const int32_t* wsta
 
 template <int kAgg, int kR, int kMinB, int S0, int S1, int S2, int S3>
 __global__ void __launch_bounds__(kStarThreads, kMinB) star_plan_kernel(const __grid_constant__ StarParams P) {
-  constexpr bool kNarrow = PlanNarrow<S0, S1, S2, S3>::value;
-  using PwT = typename std::conditional<kNarrow, uint16_t, uint32_t>::type;
+  using PwT = typename PlanEntryWord<S0, S1, S2, S3>::type;
   constexpr int kWR = plan_warp_rows(kR);
   constexpr int kTR = kConsumerWarps * kWR;
   extern __shared__ __align__(128) uint8_t dyn[];
@@ -157,7 +175,7 @@ __global__ void __launch_bounds__(kStarThreads, kMinB) star_plan_kernel(const __
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ncols = P.ncols, nst = P.nstages;
   int32_t* ring = reinterpret_cast<int32_t*>(dyn);
-  const size_t lb = plan_list_bytes(P.ndims, kR, kNarrow);
+  const size_t lb = plan_list_bytes(P.ndims, kR, (int)sizeof(PwT));
   uint8_t* lists = dyn + (size_t)nst * ncols * kTR * 4;
   uint32_t* tables = reinterpret_cast<uint32_t*>(lists + kConsumerWarps * lb);
   unsigned long long* s_sum =
