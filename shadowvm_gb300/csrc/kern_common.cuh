@@ -50,6 +50,20 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
+// A ring position: the stage of the current tile and the parity of that
+// stage's current use, advanced tile by tile, so that no loop divides its
+// 64-bit tile count by the run-time ring depth.
+struct RingPos {
+  int s = 0;
+  uint32_t phase = 0;
+  __device__ __forceinline__ void next(int nst) {
+    if (++s == nst) {
+      s = 0;
+      phase ^= 1u;
+    }
+  }
+};
+
 // 1-D bulk copy global -> shared, completion signalled as transaction bytes on `bar`.
 // dst and src 16-byte aligned, bytes a multiple of 16.
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {

@@ -340,9 +340,12 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
     const bool tma = fw == 0;
     const uint64_t pol_tab = policy_evict_last(), pol_fact = policy_evict_first();
     long long last_real = -1, last_seen = -1;  // lane 0: last tile copied / last tile waited for
-    auto issue_tile = [&](long long i) -> bool {  // lane 0 only; false on a timeout
-      const int s = (int)(i % nst);
-      if (i >= nst && !mbar_wait_bounded(&empty[s], (uint32_t)((i / nst - 1) & 1), kPolls)) return false;
+    RingPos ip;                                 // lane 0: the ring position of the next issue
+    auto issue_tile = [&](long long i) -> bool {  // lane 0 only, i = 0, 1, 2, ...; false on a timeout
+      const int s = ip.s;
+      const uint32_t ph = ip.phase;
+      ip.next(nst);
+      if (i >= nst && !mbar_wait_bounded(&empty[s], ph ^ 1u, kPolls)) return false;
       const long long t = (long long)atomicAdd(B.tile_counter, 1ull);
       if (t >= ntiles) {
         stage_tile[s] = -1;  // end of the scan
@@ -362,9 +365,10 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
     int ok = 1;
     if (tma && lane == 0) ok = issue_tile(0);
     ok = __shfl_sync(0xffffffffu, ok, 0);
-    for (long long i = 0; ok; i++) {
-      const int s = (int)(i % nst), b = (int)(i & 1);
-      bool good = mbar_wait_bounded(&full[s], (uint32_t)((i / nst) & 1), kPolls);
+    RingPos rp;
+    for (long long i = 0; ok; i++, rp.next(nst)) {
+      const int s = rp.s, b = (int)(i & 1);
+      bool good = mbar_wait_bounded(&full[s], rp.phase, kPolls);
       if (good && i >= 2) good = mbar_wait_bounded(&fill_empty[b], (uint32_t)((i / 2 - 1) & 1), kPolls);
       if (!__all_sync(0xffffffffu, good)) {
         if (lane == 0) raise_error(B.error, DERR_TIMEOUT);
@@ -422,9 +426,10 @@ __global__ void __launch_bounds__(kMBThreads, 1) mbatch_kernel(const __grid_cons
     return;
   }
 
-  for (long long i = 0;; i++) {
-    const int s = (int)(i % nst), b = (int)(i & 1);
-    const uint32_t sp = (uint32_t)((i / nst) & 1), bp = (uint32_t)((i / 2) & 1);
+  RingPos rp;
+  for (long long i = 0;; i++, rp.next(nst)) {
+    const int s = rp.s, b = (int)(i & 1);
+    const uint32_t sp = rp.phase, bp = (uint32_t)((i / 2) & 1);
     // Warp 0 waits for the tile and hands its query list (written by the
     // fill warps) to the other warps.
     if (warp == 0 && lane == 0) {

@@ -310,10 +310,10 @@ __global__ void __launch_bounds__(kStarThreads, 3) star_kernel(const __grid_cons
     // ---------------- producer: one lane issues the bulk copies
     if (lane == 0 && !P.stall_copies) {
       long long issued = 0;
-      for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, issued++) {
-        int s = (int)(issued % nst);
-        long long k = issued / nst;
-        if (k > 0 && !mbar_wait_bounded(&S.empty[s], (uint32_t)((k - 1) & 1), polls)) {
+      RingPos rp;
+      for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, issued++, rp.next(nst)) {
+        const int s = rp.s;
+        if (issued >= nst && !mbar_wait_bounded(&S.empty[s], rp.phase ^ 1u, polls)) {
           raise_error(P.error, DERR_TIMEOUT);
           break;
         }
@@ -335,10 +335,10 @@ __global__ void __launch_bounds__(kStarThreads, 3) star_kernel(const __grid_cons
     const uint32_t lt = lanemask_lt();
     uint32_t* buf = aggbuf + (size_t)warp * kAggCap * (deferred ? P.agg_words : 0);
     int cnt = 0;  // rows buffered (deferred aggregation)
-    long long i = 0;
-    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
-      int s = (int)(i % nst);
-      if (!mbar_wait_bounded(&S.full[s], (uint32_t)((i / nst) & 1), polls)) {
+    RingPos rp;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, rp.next(nst)) {
+      const int s = rp.s;
+      if (!mbar_wait_bounded(&S.full[s], rp.phase, polls)) {
         raise_error(P.error, DERR_TIMEOUT);
         break;
       }
@@ -615,10 +615,10 @@ __global__ void __launch_bounds__(kStarThreads, 2) batch_kernel(const __grid_con
   if (warp == kConsumerWarps) {
     if (lane == 0) {
       long long issued = 0;
-      for (;; issued++) {
-        const int s = (int)(issued % nst);
-        const long long k = issued / nst;
-        if (k > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)((k - 1) & 1), kWaitPolls)) {
+      RingPos rp;
+      for (;; issued++, rp.next(nst)) {
+        const int s = rp.s;
+        if (issued >= nst && !mbar_wait_bounded(&empty[s], rp.phase ^ 1u, kWaitPolls)) {
           raise_error(B.error, DERR_TIMEOUT);
           break;
         }
@@ -645,9 +645,9 @@ __global__ void __launch_bounds__(kStarThreads, 2) batch_kernel(const __grid_con
   }
   const WarpList L = warp_list(lists, warp, kMaxDims);
   const uint32_t lt = lanemask_lt();
-  for (long long i = 0;; i++) {
-    const int s = (int)(i % nst);
-    if (!mbar_wait_bounded(&full[s], (uint32_t)((i / nst) & 1), kWaitPolls)) {
+  for (RingPos rp;; rp.next(nst)) {
+    const int s = rp.s;
+    if (!mbar_wait_bounded(&full[s], rp.phase, kWaitPolls)) {
       raise_error(B.error, DERR_TIMEOUT);
       break;
     }

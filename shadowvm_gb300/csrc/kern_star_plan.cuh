@@ -213,10 +213,10 @@ __global__ void __launch_bounds__(kStarThreads, kMinB) star_plan_kernel(const __
     // ---------------- producer: one lane issues the bulk copies
     if (lane == 0 && !P.stall_copies) {
       long long issued = 0;
-      for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, issued++) {
-        const int s = (int)(issued % nst);
-        const long long k = issued / nst;
-        if (k > 0 && !mbar_wait_bounded(&S.empty[s], (uint32_t)((k - 1) & 1), polls)) {
+      RingPos rp;
+      for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, issued++, rp.next(nst)) {
+        const int s = rp.s;
+        if (issued >= nst && !mbar_wait_bounded(&S.empty[s], rp.phase ^ 1u, polls)) {
           raise_error(P.error, DERR_TIMEOUT);
           break;
         }
@@ -242,10 +242,10 @@ __global__ void __launch_bounds__(kStarThreads, kMinB) star_plan_kernel(const __
     const int W = P.agg_words;
     uint32_t* buf = aggbuf + (size_t)warp * kAggCap * W;
     int cnt = 0;  // rows buffered
-    long long i = 0;
-    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
-      const int s = (int)(i % nst);
-      if (!mbar_wait_bounded(&S.full[s], (uint32_t)((i / nst) & 1), polls)) {
+    RingPos rp;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, rp.next(nst)) {
+      const int s = rp.s;
+      if (!mbar_wait_bounded(&S.full[s], rp.phase, polls)) {
         raise_error(P.error, DERR_TIMEOUT);
         break;
       }
