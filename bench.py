@@ -306,8 +306,11 @@ def ours_arm(args):
     rows = w.fact_rows
     eng = Engine(device=local, tuple_per_bulk=w.tuple_per_bulk, join_mode=args.join_mode)
     if args.pin:
-        r, mb, st, sg = (int(v) for v in args.pin.split(","))
+        pins = [int(v) for v in args.pin.split(",")]
+        r, mb, st, sg = pins[:4]
         eng.pin_launch(r, st, sg, blocks_per_sm=mb)
+        if len(pins) > 4:
+            eng.pin_list_after(pins[4])
     W.load_engine(eng, w, row0=rank * rows)
     t_build0 = time.time()
     for p in w.dim_pipelines:
@@ -731,8 +734,9 @@ def main():
     ap.add_argument("--inflight", type=int, default=2, help="config 4: folds begun and not complete, at most")
     ap.add_argument("--loader", action="store_true", help="measure the text Loader instead")
     ap.add_argument("--pin", default=None,
-                    help="rows_per_lane,blocks_per_sm,ring_stages,tables_staged: pin the scan's launch "
-                         "configuration (svm_pin_launch), e.g. for a profile of one variant")
+                    help="rows_per_lane,blocks_per_sm,ring_stages,tables_staged[,list_after]: pin the scan's "
+                         "launch configuration (svm_pin_launch, svm_pin_list_after), e.g. for a profile of "
+                         "one variant")
     ap.add_argument("--join-mode", default="ref_compat", choices=["ref_compat", "exact"])
     args = ap.parse_args()
     if args.warmup < 3:

@@ -320,6 +320,13 @@ svm_status svm_scan_aggregate_noalloc(svm_ctx* ctx, const svm_noalloc_scan* q, i
  * 1024 threads a block, com/cpp/com.cu:19-20). */
 svm_status svm_pin_launch(svm_ctx* ctx, int rows_per_lane, int blocks_per_sm, int ring_stages, int tables_staged);
 
+/* Narrows, in the same way, the compiled kernel's row-list form:
+ * list_after -1 (any), 0..2 (after that filter step each warp's live rows
+ * become a list and the later steps run over the list only) or 3 (every
+ * step runs over all rows, predicated).  Only some plan shapes have the list
+ * forms compiled.  No counterpart in the reference. */
+svm_status svm_pin_list_after(svm_ctx* ctx, int list_after);
+
 /* The same for the merged batch kernel of svm_run_batch / svm_batch_begin:
  * consumer_warps 0 (any), 28 or 24 of its 32 warps (the others look rows
  * up in the merged tables and issue the bulk copies), ring_stages 0 (any)

@@ -23,7 +23,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}"]
 CU_FLAGS = ["--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
-SOURCES = ["capi.cpp", "pipeline.cpp", "expr.cpp", "strdict.cpp", "kern_util.cu", "kern_dim.cu", "kern_star.cu", "kern_star_plan.cu", "kern_star_plan_mix.cu", "kern_star_plan_mix2.cu", "kern_star_plan_mix3.cu", "kern_mbatch.cu", "kern_load.cu",
+SOURCES = ["capi.cpp", "pipeline.cpp", "expr.cpp", "strdict.cpp", "kern_util.cu", "kern_dim.cu", "kern_star.cu", "kern_star_plan.cu", "kern_star_plan_mix.cu", "kern_star_plan_mix2.cu", "kern_star_plan_mix3.cu", "kern_star_plan_list.cu", "kern_mbatch.cu", "kern_load.cu",
            "kern_noalloc.cu"]
 HEADERS = ["svm_internal.h", "kern_common.cuh", "kern_star_common.cuh", "kern_star_plan.cuh", "kernels.h", "ctx.h", "expr.h", "strdict.h"]
 

@@ -123,6 +123,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "svm_test_device_wait": (I, [P, ctypes.c_uint, I]),
         "svm_last_launch": (I, [P, ctypes.c_char_p, U64]),
         "svm_pin_launch": (I, [P, I, I, I, I]),
+        "svm_pin_list_after": (I, [P, I]),
         "svm_pin_batch_launch": (I, [P, I, I]),
         "svm_scan_aggregate_noalloc": (I, [P, ctypes.POINTER(svm_noalloc_scan), ctypes.POINTER(P),
                                            ctypes.POINTER(P), U64, ctypes.POINTER(U64)]),

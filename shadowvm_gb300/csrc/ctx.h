@@ -174,6 +174,7 @@ struct Ctx {
     int swap = -1;
     int rows = 0;
     int minb = 0;   // compiled kernel: the blocks per SM it is compiled for
+    int list = 3;   // compiled kernel: the step after which later steps run over a row list (3: none)
   };
   // Pinned launch choices (svm_pin_launch): kernel rows per lane (-1: any,
   // 0: the interpreted kernel, 4 or 8: the compiled one), the blocks per SM
@@ -181,6 +182,8 @@ struct Ctx {
   // staged (-1: any).  A pin narrows the candidates; the rule or
   // the tuner picks among those left.
   int pin_rows = -1, pin_minb = 0, pin_stages = 0, pin_staged = -1;
+  // Pinned row-list step of the compiled kernel (svm_pin_list_after; -1: any).
+  int pin_list = -1;
   // Pinned merged-batch launch choices (svm_pin_batch_launch): consumer warps
   // (0: any, 28 or 24) and ring stages (0: any).
   int pin_batch_cw = 0, pin_batch_stages = 0;

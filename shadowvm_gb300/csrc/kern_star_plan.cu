@@ -66,6 +66,10 @@ extern const int kPlansMix2Count;
 // The date + part shapes with a presence prefilter (kern_star_plan_mix3.cu).
 extern const PlanEntry kPlansMix3[];
 extern const int kPlansMix3Count;
+// Shapes whose later steps run over a list of the live rows
+// (kern_star_plan_list.cu).
+extern const PlanEntry kPlansList[];
+extern const int kPlansListCount;
 
 namespace {
 
@@ -83,7 +87,7 @@ bool plan_is_compilable(const StarParams& p) {
   return true;
 }
 
-const PlanEntry* find_plan(const StarParams& p, int rows, int minb) {
+const PlanEntry* find_plan(const StarParams& p, int rows, int minb, int list_after) {
   if (!plan_is_compilable(p)) return nullptr;
   int code[4];
   for (int k = 0; k < 4; k++) {
@@ -91,8 +95,8 @@ const PlanEntry* find_plan(const StarParams& p, int rows, int minb) {
     if (code[k] < 0) return nullptr;
   }
   auto match = [&](const PlanEntry& e) {
-    return e.agg == p.agg && e.rows == rows && e.minb == minb && e.s[0] == code[0] && e.s[1] == code[1] &&
-           e.s[2] == code[2] && e.s[3] == code[3];
+    return e.agg == p.agg && e.rows == rows && e.minb == minb && e.list_after == list_after &&
+           e.s[0] == code[0] && e.s[1] == code[1] && e.s[2] == code[2] && e.s[3] == code[3];
   };
   for (const PlanEntry& e : kPlans)
     if (match(e)) return &e;
@@ -102,6 +106,8 @@ const PlanEntry* find_plan(const StarParams& p, int rows, int minb) {
     if (match(kPlansMix2[i])) return &kPlansMix2[i];
   for (int i = 0; i < kPlansMix3Count; i++)
     if (match(kPlansMix3[i])) return &kPlansMix3[i];
+  for (int i = 0; i < kPlansListCount; i++)
+    if (match(kPlansList[i])) return &kPlansList[i];
   return nullptr;
 }
 
@@ -118,8 +124,8 @@ int star_plan_code(const StarParams& p, int k) {
   return (st.smem_word_off >= 0 ? SC_SMEM : SC_L2) | lg << 2 | (ranged ? 32 : 0);
 }
 
-bool star_plan_available(const StarParams& p, int rows_per_lane, int min_blocks) {
-  return find_plan(p, rows_per_lane, min_blocks) != nullptr;
+bool star_plan_available(const StarParams& p, int rows_per_lane, int min_blocks, int list_after) {
+  return find_plan(p, rows_per_lane, min_blocks, list_after) != nullptr;
 }
 
 size_t star_plan_smem_bytes(const StarParams& p, int rows_per_lane) {
@@ -136,8 +142,8 @@ size_t star_plan_smem_bytes(const StarParams& p, int rows_per_lane) {
   return b;
 }
 
-int star_plan_blocks_per_sm(const StarParams& p, int rows_per_lane, int min_blocks, size_t smem) {
-  const PlanEntry* e = find_plan(p, rows_per_lane, min_blocks);
+int star_plan_blocks_per_sm(const StarParams& p, int rows_per_lane, int min_blocks, int list_after, size_t smem) {
+  const PlanEntry* e = find_plan(p, rows_per_lane, min_blocks, list_after);
   if (!e) return 0;
   if (allow_dynamic_smem(e->fn, 210 * 1024) != cudaSuccess) return 0;
   int per_sm = 0;
@@ -145,8 +151,8 @@ int star_plan_blocks_per_sm(const StarParams& p, int rows_per_lane, int min_bloc
   return per_sm;
 }
 
-int star_plan_grid_size(const StarParams& p, int rows_per_lane, int min_blocks, size_t smem) {
-  int per_sm = star_plan_blocks_per_sm(p, rows_per_lane, min_blocks, smem);
+int star_plan_grid_size(const StarParams& p, int rows_per_lane, int min_blocks, int list_after, size_t smem) {
+  int per_sm = star_plan_blocks_per_sm(p, rows_per_lane, min_blocks, list_after, smem);
   if (per_sm < 1) per_sm = 1;
   const long long tr = (long long)kConsumerWarps * plan_warp_rows(rows_per_lane);
   long long tiles = (p.row_end - (p.row_begin & ~3ll) + tr - 1) / tr;
@@ -155,9 +161,9 @@ int star_plan_grid_size(const StarParams& p, int rows_per_lane, int min_blocks, 
   return (int)(tiles < cap ? tiles : cap);
 }
 
-cudaError_t launch_star_plan(const StarParams& p, int rows_per_lane, int min_blocks, int grid, size_t smem,
-                             cudaStream_t s) {
-  const PlanEntry* e = find_plan(p, rows_per_lane, min_blocks);
+cudaError_t launch_star_plan(const StarParams& p, int rows_per_lane, int min_blocks, int list_after, int grid,
+                             size_t smem, cudaStream_t s) {
+  const PlanEntry* e = find_plan(p, rows_per_lane, min_blocks, list_after);
   if (!e) return cudaErrorInvalidValue;
   note_launch();
   void* args[] = {const_cast<StarParams*>(&p)};

@@ -165,7 +165,99 @@ __device__ __forceinline__ void plan_step_if(const Step& st, const int32_t* wsta
   plan_step<kCode, kR, PwT>(st, wstage, tables, L, lane, mask);
 }
 
-template <int kAgg, int kR, int kMinB, int S0, int S1, int S2, int S3>
+// The warp's live rows after the dense steps, as a list of row offsets in
+// row order (L.row); returns their count.  Lane L's rows of a 128-row slice
+// are 4L..4L+3, so a lane's place in the list is the live rows of the lanes
+// before it: their counts (0..4) summed from three ballots of the count bits.
+template <int kR, typename PwT>
+__device__ __forceinline__ int plan_sorted_list(const PlanList<kR, PwT>& L, int lane, uint32_t lt, uint32_t mask) {
+  int n = 0;
+#pragma unroll
+  for (int q = 0; q < kR / 4; q++) {
+    const uint32_t m4 = (mask >> (4 * q)) & 15u;
+    const uint32_t c = (uint32_t)__popc(m4);
+    const uint32_t b0 = __ballot_sync(0xffffffffu, c & 1u), b1 = __ballot_sync(0xffffffffu, c & 2u),
+                   b2 = __ballot_sync(0xffffffffu, c & 4u);
+    int pos = n + __popc(b0 & lt) + 2 * __popc(b1 & lt) + 4 * __popc(b2 & lt);
+#pragma unroll
+    for (int jj = 0; jj < 4; jj++)
+      if ((m4 >> jj) & 1u) L.row[pos++] = (uint16_t)(q * 128 + lane * 4 + jj);
+    n += __popc(b0) + 2 * __popc(b1) + 4 * __popc(b2);
+  }
+  __syncwarp();
+  return n;
+}
+
+// One compiled filter step over the warp's list of live rows (n of them):
+// lane L takes entries L, L + 32, L + 64 and L + 96 of each 128, so four
+// probe loads are in flight per lane; the survivors are compacted in place,
+// in row order, and each keeps its table entry (by row offset) when the
+// table has a payload.  Returns the survivors' count.
+template <int kCode, int kR, typename PwT>
+__device__ __forceinline__ int plan_list_step(const Step& st, const int32_t* wstage, const uint32_t* tables,
+                                              const PlanList<kR, PwT>& L, int lane, uint32_t lt, int n) {
+  using C = StepCode<kCode>;
+  if (C::kind == SC_NONE || n == 0) return n;
+  constexpr int kTR = kConsumerWarps * plan_warp_rows(kR);
+  constexpr int kU = 4;
+  const int32_t* col = wstage + st.col * kTR;
+  int out = 0;
+  for (int r0 = 0; r0 < n; r0 += 32 * kU) {
+    int row[kU];
+    bool live[kU];
+    uint32_t key[kU], e[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int i = r0 + u * 32 + lane;
+      live[u] = i < n;
+      row[u] = live[u] ? (int)L.row[i] : 0;
+      key[u] = (uint32_t)col[row[u]];
+      e[u] = 0u;
+    }
+    if (C::kind == SC_RANGE || C::ranged) {
+      const uint32_t lo = (uint32_t)st.lo, span = (uint32_t)st.hi - (uint32_t)st.lo;
+#pragma unroll
+      for (int u = 0; u < kU; u++) live[u] = live[u] && key[u] - lo <= span;
+    }
+    if (C::probe) {
+      const uint32_t kmin = (uint32_t)st.key_min, span = st.span;
+      uint32_t word[kU], sh[kU];
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        const uint32_t idx = key[u] - kmin;
+        live[u] = live[u] && idx < span;
+        const uint32_t bit = idx << C::bits_log2;
+        sh[u] = bit & 31u;
+        const uint32_t wi = bit >> 5;
+        if (C::kind == SC_SMEM)
+          word[u] = live[u] ? tables[st.smem_word_off + wi] : 0u;
+        else
+          word[u] = live[u] ? __ldg(st.words + wi) : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        e[u] = C::bits == 32 ? word[u] : (word[u] >> sh[u]) & ((1u << (C::bits & 31)) - 1u);
+        live[u] = live[u] && (e[u] & 1u);
+      }
+    }
+    __syncwarp();  // every entry of this round is read before any is overwritten
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const uint32_t b = __ballot_sync(0xffffffffu, live[u]);
+      if (live[u]) {
+        L.row[out + __popc(b & lt)] = (uint16_t)row[u];
+        if (C::probe && C::bits > 1) L.pw(st.dim)[row[u]] = (PwT)e[u];
+      }
+      out += __popc(b);
+    }
+    __syncwarp();
+  }
+  return out;
+}
+
+// kC: the step after which the warp's live rows become a list (0..2: the
+// later steps run over the list; 3: every step runs over all the warp's rows).
+template <int kAgg, int kR, int kMinB, int kC, int S0, int S1, int S2, int S3>
 __global__ void __launch_bounds__(kStarThreads, kMinB) star_plan_kernel(const __grid_constant__ StarParams P) {
   using PwT = typename PlanEntryWord<S0, S1, S2, S3>::type;
   constexpr int kWR = plan_warp_rows(kR);
@@ -262,20 +354,32 @@ __global__ void __launch_bounds__(kStarThreads, kMinB) star_plan_kernel(const __
           mask |= (uint32_t)(r >= P.row_begin && r < P.row_end) << j;
         }
       }
-      plan_step_if<S0, kR, PwT>(P.steps[0], wstage, tables, L, lane, mask);
-      plan_step_if<S1, kR, PwT>(P.steps[1], wstage, tables, L, lane, mask);
-      plan_step_if<S2, kR, PwT>(P.steps[2], wstage, tables, L, lane, mask);
-      plan_step_if<S3, kR, PwT>(P.steps[3], wstage, tables, L, lane, mask);
-
-      // ---- the survivors as a list of row offsets
       int n = 0;
+      plan_step_if<S0, kR, PwT>(P.steps[0], wstage, tables, L, lane, mask);
+      if (kC == 0) n = plan_sorted_list<kR, PwT>(L, lane, lt, mask);
+      if (kC < 1)
+        n = plan_list_step<S1, kR, PwT>(P.steps[1], wstage, tables, L, lane, lt, n);
+      else
+        plan_step_if<S1, kR, PwT>(P.steps[1], wstage, tables, L, lane, mask);
+      if (kC == 1) n = plan_sorted_list<kR, PwT>(L, lane, lt, mask);
+      if (kC < 2)
+        n = plan_list_step<S2, kR, PwT>(P.steps[2], wstage, tables, L, lane, lt, n);
+      else
+        plan_step_if<S2, kR, PwT>(P.steps[2], wstage, tables, L, lane, mask);
+      if (kC == 2) n = plan_sorted_list<kR, PwT>(L, lane, lt, mask);
+      if (kC < 3) {
+        n = plan_list_step<S3, kR, PwT>(P.steps[3], wstage, tables, L, lane, lt, n);
+      } else {
+        plan_step_if<S3, kR, PwT>(P.steps[3], wstage, tables, L, lane, mask);
+        // ---- the survivors as a list of row offsets
 #pragma unroll
-      for (int j = 0; j < kR; j++) {
-        const uint32_t b = __ballot_sync(0xffffffffu, (mask >> j) & 1u);
-        if ((mask >> j) & 1u) L.row[n + __popc(b & lt)] = (uint16_t)plan_row<kR>(lane, j);
-        n += __popc(b);
+        for (int j = 0; j < kR; j++) {
+          const uint32_t b = __ballot_sync(0xffffffffu, (mask >> j) & 1u);
+          if ((mask >> j) & 1u) L.row[n + __popc(b & lt)] = (uint16_t)plan_row<kR>(lane, j);
+          n += __popc(b);
+        }
+        __syncwarp();
       }
-      __syncwarp();
       // ---- their operand words into the warp's buffer, aggregated 32 rows at a time
       for (int done = 0; done < n;) {
         const int take = n - done < kAggCap - cnt ? n - done : kAggCap - cnt;
@@ -310,7 +414,7 @@ constexpr int smem(int bits_log2) { return SC_SMEM | bits_log2 << 2; }
 constexpr int l2(int bits_log2) { return SC_L2 | bits_log2 << 2; }
 
 struct PlanEntry {
-  int agg, rows, minb, s[4];
+  int agg, rows, minb, list_after, s[4];
   const void* fn;
 };
 
@@ -318,8 +422,16 @@ struct PlanEntry {
 }  // namespace svm
 
 #define SVM_PLAN(AGG, R, MB, A, B, C, D)                                             \
-  {AGG, R, MB, {A, B, C, D},                                                         \
-   reinterpret_cast<const void*>(&::svm::plan::star_plan_kernel<AGG, R, MB, A, B, C, D>)}
+  {AGG, R, MB, 3, {A, B, C, D},                                                      \
+   reinterpret_cast<const void*>(&::svm::plan::star_plan_kernel<AGG, R, MB, 3, A, B, C, D>)}
+// A shape with 8 rows per lane for 2 blocks per SM whose live rows become a
+// list after step KC.
+#define SVM_PLAN_LIST(AGG, KC, A, B, C, D)                                          \
+  {AGG, 8, 2, KC, {A, B, C, D},                                                      \
+   reinterpret_cast<const void*>(&::svm::plan::star_plan_kernel<AGG, 8, 2, KC, A, B, C, D>)}
 // Each shape with 4 rows per lane for 3 or 4 blocks per SM, and 8 rows per lane for 2.
 #define SVM_PLAN_R(AGG, A, B, C, D) \
   SVM_PLAN(AGG, 4, 3, A, B, C, D), SVM_PLAN(AGG, 4, 4, A, B, C, D), SVM_PLAN(AGG, 8, 2, A, B, C, D)
+// The same, and the form with 8 rows per lane whose steps after the first
+// run over a list of the live rows.
+#define SVM_PLAN_RL(AGG, A, B, C, D) SVM_PLAN_R(AGG, A, B, C, D), SVM_PLAN_LIST(AGG, 0, A, B, C, D)

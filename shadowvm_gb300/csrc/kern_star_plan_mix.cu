@@ -9,14 +9,14 @@ namespace svm {
 using namespace plan;
 
 extern const PlanEntry kPlansMix1[] = {
-    SVM_PLAN_R(AGG_SCALAR, R_, R_, R_, smem(0)),
-    SVM_PLAN_R(AGG_SCALAR, R_, R_, smem(0), R_),
-    SVM_PLAN_R(AGG_SCALAR, R_, R_, R_, l2(0)),
-    SVM_PLAN_R(AGG_SCALAR, R_, R_, l2(0), R_),
-    SVM_PLAN_R(AGG_DENSE_SMEM, R_, l2(3), smem(2), SC_NONE),
-    SVM_PLAN_R(AGG_DENSE_SMEM, l2(3), R_, smem(2), SC_NONE),
-    SVM_PLAN_R(AGG_DENSE_SMEM, R_, l2(3), l2(2), SC_NONE),
-    SVM_PLAN_R(AGG_DENSE_SMEM, l2(3), R_, l2(2), SC_NONE),
+    SVM_PLAN_RL(AGG_SCALAR, R_, R_, R_, smem(0)),
+    SVM_PLAN_RL(AGG_SCALAR, R_, R_, smem(0), R_),
+    SVM_PLAN_RL(AGG_SCALAR, R_, R_, R_, l2(0)),
+    SVM_PLAN_RL(AGG_SCALAR, R_, R_, l2(0), R_),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, R_, l2(3), smem(2), SC_NONE),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, l2(3), R_, smem(2), SC_NONE),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, R_, l2(3), l2(2), SC_NONE),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, l2(3), R_, l2(2), SC_NONE),
 };
 extern const int kPlansMix1Count = (int)(sizeof(kPlansMix1) / sizeof(kPlansMix1[0]));
 

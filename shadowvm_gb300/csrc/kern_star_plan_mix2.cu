@@ -8,12 +8,12 @@ namespace svm {
 using namespace plan;
 
 extern const PlanEntry kPlansMix2[] = {
-    SVM_PLAN_R(AGG_DENSE_SMEM, R_, smem(2), l2(2), l2(2)),
-    SVM_PLAN_R(AGG_DENSE_SMEM, smem(2), R_, l2(2), l2(2)),
-    SVM_PLAN_R(AGG_DENSE_SMEM, smem(2), l2(2), l2(2), R_),
-    SVM_PLAN_R(AGG_DENSE_SMEM, R_, l2(2), l2(2), l2(2)),
-    SVM_PLAN_R(AGG_DENSE_SMEM, l2(2), R_, l2(2), l2(2)),
-    SVM_PLAN_R(AGG_DENSE_SMEM, l2(2), l2(2), l2(2), R_),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, R_, smem(2), l2(2), l2(2)),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, smem(2), R_, l2(2), l2(2)),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, smem(2), l2(2), l2(2), R_),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, R_, l2(2), l2(2), l2(2)),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, l2(2), R_, l2(2), l2(2)),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, l2(2), l2(2), l2(2), R_),
 };
 extern const int kPlansMix2Count = (int)(sizeof(kPlansMix2) / sizeof(kPlansMix2[0]));
 

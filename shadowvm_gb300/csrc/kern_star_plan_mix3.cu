@@ -9,15 +9,15 @@ namespace svm {
 using namespace plan;
 
 extern const PlanEntry kPlansMix3[] = {
-    SVM_PLAN_R(AGG_DENSE_SMEM, l2(0), smem(2), l2(3), SC_NONE),
-    SVM_PLAN_R(AGG_DENSE_SMEM, smem(0), smem(2), l2(3), SC_NONE),
-    SVM_PLAN_R(AGG_DENSE_SMEM, l2(0), l2(2), l2(3), SC_NONE),
-    SVM_PLAN_R(AGG_DENSE_SMEM, R_, l2(0), smem(2), l2(3)),
-    SVM_PLAN_R(AGG_DENSE_SMEM, l2(0), R_, smem(2), l2(3)),
-    SVM_PLAN_R(AGG_DENSE_SMEM, R_, smem(0), smem(2), l2(3)),
-    SVM_PLAN_R(AGG_DENSE_SMEM, smem(0), R_, smem(2), l2(3)),
-    SVM_PLAN_R(AGG_DENSE_SMEM, R_, l2(0), l2(2), l2(3)),
-    SVM_PLAN_R(AGG_DENSE_SMEM, l2(0), R_, l2(2), l2(3)),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, l2(0), smem(2), l2(3), SC_NONE),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, smem(0), smem(2), l2(3), SC_NONE),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, l2(0), l2(2), l2(3), SC_NONE),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, R_, l2(0), smem(2), l2(3)),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, l2(0), R_, smem(2), l2(3)),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, R_, smem(0), smem(2), l2(3)),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, smem(0), R_, smem(2), l2(3)),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, R_, l2(0), l2(2), l2(3)),
+    SVM_PLAN_RL(AGG_DENSE_SMEM, l2(0), R_, l2(2), l2(3)),
 };
 extern const int kPlansMix3Count = (int)(sizeof(kPlansMix3) / sizeof(kPlansMix3[0]));
 

@@ -92,14 +92,16 @@ size_t star_smem_bytes(const StarParams& p);
 // The fused scan compiled per plan shape (kern_star_plan.cu): available for
 // plans of at most four steps (ranges and dense-table probes), no bytecode,
 // and an instantiated shape; rows_per_lane 4 (for 3 or 4 blocks per SM) or
-// 8 (for 2 blocks per SM), min_blocks the blocks per SM it is compiled for.
+// 8 (for 2 blocks per SM), min_blocks the blocks per SM it is compiled for,
+// list_after the step after which the later steps run over a list of the
+// warp's live rows (3: none do).
 int star_plan_code(const StarParams& p, int k);  // step k's code (-1: not compilable)
-bool star_plan_available(const StarParams& p, int rows_per_lane, int min_blocks);
+bool star_plan_available(const StarParams& p, int rows_per_lane, int min_blocks, int list_after);
 size_t star_plan_smem_bytes(const StarParams& p, int rows_per_lane);
-int star_plan_blocks_per_sm(const StarParams& p, int rows_per_lane, int min_blocks, size_t smem);
-int star_plan_grid_size(const StarParams& p, int rows_per_lane, int min_blocks, size_t smem);
-cudaError_t launch_star_plan(const StarParams& p, int rows_per_lane, int min_blocks, int grid, size_t smem,
-                             cudaStream_t s);
+int star_plan_blocks_per_sm(const StarParams& p, int rows_per_lane, int min_blocks, int list_after, size_t smem);
+int star_plan_grid_size(const StarParams& p, int rows_per_lane, int min_blocks, int list_after, size_t smem);
+cudaError_t launch_star_plan(const StarParams& p, int rows_per_lane, int min_blocks, int list_after, int grid,
+                             size_t smem, cudaStream_t s);
 // Compact non-empty groups in key order: writes keys (nkeys int32 columns),
 // metric columns (int64 or int32 per `wide`), and out_count.
 cudaError_t launch_finalize_dense(const StarParams& p, int32_t* const* key_out, void* const* met_out,

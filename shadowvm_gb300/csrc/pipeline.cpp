@@ -1098,7 +1098,8 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   const std::vector<Step> steps0(P.steps, P.steps + P.nsteps);
   const std::string shape = x->cfg.autotune ? star_shape_key(P) + "|pin" + std::to_string(x->pin_rows) + "," +
                                                  std::to_string(x->pin_minb) + "," + std::to_string(x->pin_stages) +
-                                                 "," + std::to_string(x->pin_staged)
+                                                 "," + std::to_string(x->pin_staged) + "," +
+                                                 std::to_string(x->pin_list)
                                            : std::string();  // as planned
   // The compiled kernel reads the columns no filter step needs only at the
   // surviving rows (late columns); the interpreted kernel stages them all.
@@ -1115,10 +1116,10 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   };
   auto smem_of = [&](const Cand& c) { return c.rows ? star_plan_smem_bytes(P, c.rows) : star_smem_bytes(P); };
   auto grid_of = [&](const Cand& c, size_t sm) {
-    return c.rows ? star_plan_grid_size(P, c.rows, c.minb, sm) : star_grid_size(P, sm);
+    return c.rows ? star_plan_grid_size(P, c.rows, c.minb, c.list, sm) : star_grid_size(P, sm);
   };
   auto launch = [&](const Cand& c, size_t sm) {
-    return c.rows ? launch_star_plan(P, c.rows, c.minb, grid_of(c, sm), sm, x->stream)
+    return c.rows ? launch_star_plan(P, c.rows, c.minb, c.list, grid_of(c, sm), sm, x->stream)
                   : launch_star(P, grid_of(c, sm), star_block_size(), sm, x->stream);
   };
   std::vector<int> swaps = {-1};
@@ -1136,31 +1137,36 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   for (int sw : swaps)
     for (int staged = 1; staged >= (any_staged ? 0 : 1); staged--)
       for (const auto& rm : {std::make_pair(4, 3), std::make_pair(4, 4), std::make_pair(8, 2), std::make_pair(0, 0)})
-        for (int nst = kStages; nst >= 2; nst--) {
-          const int rows = rm.first;
-          if ((x->pin_rows >= 0 && rows != x->pin_rows) || (x->pin_stages && nst != x->pin_stages) ||
-              (x->pin_staged >= 0 && staged != x->pin_staged) || (x->pin_minb && rm.second != x->pin_minb))
-            continue;
-          Cand c;
-          c.nst = nst;
-          c.staged = staged != 0;
-          c.swap = sw;
-          c.rows = rows;
-          c.minb = rm.second;
-          configure(c);
-          if (rows && !star_plan_available(P, rows, c.minb)) continue;
-          const size_t sm = smem_of(c);
-          if (sm > 200 * 1024) continue;
-          const int blocks = rows ? star_plan_blocks_per_sm(P, rows, c.minb, sm) : star_blocks_per_sm(P, sm);
-          // a kernel built for 4 blocks per SM where fewer fit gains nothing over the one built for 3
-          if (blocks > 0 && !(rows && c.minb > 3 && blocks < c.minb)) cands.push_back({c, blocks});
-        }
+        for (int nst = kStages; nst >= 2; nst--)
+          for (int la = 3; la >= 0; la--) {
+            const int rows = rm.first;
+            if ((x->pin_rows >= 0 && rows != x->pin_rows) || (x->pin_stages && nst != x->pin_stages) ||
+                (x->pin_staged >= 0 && staged != x->pin_staged) || (x->pin_minb && rm.second != x->pin_minb) ||
+                (x->pin_list >= 0 && la != x->pin_list) || (!rows && la != 3))
+              continue;
+            Cand c;
+            c.nst = nst;
+            c.staged = staged != 0;
+            c.swap = sw;
+            c.rows = rows;
+            c.minb = rm.second;
+            c.list = la;
+            configure(c);
+            if (rows && !star_plan_available(P, rows, c.minb, la)) continue;
+            const size_t sm = smem_of(c);
+            if (sm > 200 * 1024) continue;
+            const int blocks = rows ? star_plan_blocks_per_sm(P, rows, c.minb, la, sm) : star_blocks_per_sm(P, sm);
+            // a kernel built for 4 blocks per SM where fewer fit gains nothing over the one built for 3
+            if (blocks > 0 && !(rows && c.minb > 3 && blocks < c.minb)) cands.push_back({c, blocks});
+          }
   if (cands.empty())
-    return x->fail(SVM_E_UNSUPPORTED, x->pin_rows >= 0 || x->pin_minb || x->pin_stages || x->pin_staged >= 0
+    return x->fail(SVM_E_UNSUPPORTED, x->pin_rows >= 0 || x->pin_minb || x->pin_stages || x->pin_staged >= 0 ||
+                                              x->pin_list >= 0
                                           ? "no launch configuration of this plan fits the pinned choices"
                                           : "shared-memory plan too large");
   auto rule_rank = [](const Fit& f) {  // larger is preferred
-    return (f.c.rows == 4 ? 2 : f.c.rows == 8 ? 1 : 0) * 1000000 + f.blocks * 1000 + f.c.nst * 10 + (f.c.staged ? 1 : 0);
+    return (f.c.rows == 4 ? 2 : f.c.rows == 8 ? 1 : 0) * 10000000 + f.c.list * 1000000 + f.blocks * 1000 +
+           f.c.nst * 10 + (f.c.staged ? 1 : 0);
   };
   Cand pick = cands[0].c;
   int best_rank = -1;
@@ -1218,6 +1224,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
     x->last_launch = std::string("{\"kernel\": \"") + (pick.rows ? "compiled plan" : "interpreted") +
                      "\", \"rows_per_lane\": " + std::to_string(pick.rows ? pick.rows : 4) +
                      ", \"blocks_per_sm_compiled_for\": " + std::to_string(pick.minb ? pick.minb : 3) +
+                     ", \"list_after_step\": " + std::to_string(pick.rows ? pick.list : 3) +
                      ", \"ring_stages\": " + std::to_string(pick.nst) + ", \"tables_staged\": " +
                      (pick.staged ? "true" : "false") + ", \"steps\": \"" + steps + "\", \"grid\": " +
                      std::to_string(grid) + ", \"block\": " + std::to_string(star_block_size()) +

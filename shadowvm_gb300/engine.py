@@ -244,6 +244,12 @@ class Engine:
         the defaults lift every pin."""
         self._check(self.lib.svm_pin_launch(self.h, rows_per_lane, blocks_per_sm, ring_stages, tables_staged))
 
+    def pin_list_after(self, list_after: int = -1):
+        """Narrows the compiled scan's row-list form (svm_pin_list_after):
+        -1 any, 0..2 the step after which later steps run over a list of
+        the live rows, 3 none."""
+        self._check(self.lib.svm_pin_list_after(self.h, list_after))
+
     def pin_batch_launch(self, consumer_warps: int = 0, ring_stages: int = 0):
         """Narrows the merged batch kernel's launch configurations
         (svm_pin_batch_launch); the defaults lift every pin."""

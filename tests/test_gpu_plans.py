@@ -46,22 +46,31 @@ def test_every_launch_variant_equals_the_reference(engine_factory, name):
     for rows, minb in ((4, 3), (4, 4), (8, 2), (0, 0)):
         for stages in (2, 3):
             for staged in (1, 0):
-                eng.pin_launch(rows, stages, staged, blocks_per_sm=minb)
-                try:
-                    eng.run(w.query)
-                except SvmError as e:
-                    assert rows != 0, e  # the interpreted kernel takes every plan
-                    continue
-                got = eng.result(w.query.id, w.key_num)
-                launch = eng.last_launch()
-                assert launch["ring_stages"] == stages
-                kernels.add((launch["kernel"], launch["rows_per_lane"]))
-                np.testing.assert_array_equal(got[0], gk, err_msg=f"{rows} rows, {stages} stages, staged {staged}")
-                np.testing.assert_array_equal(got[1], gs, err_msg=f"{rows} rows, {stages} stages, staged {staged}")
+                for list_after in ((3, 0, 1) if rows == 8 else (-1,)):
+                    eng.pin_launch(rows, stages, staged, blocks_per_sm=minb)
+                    eng.pin_list_after(list_after)
+                    try:
+                        eng.run(w.query)
+                    except SvmError as e:
+                        assert rows != 0, e  # the interpreted kernel takes every plan
+                        continue
+                    got = eng.result(w.query.id, w.key_num)
+                    launch = eng.last_launch()
+                    assert launch["ring_stages"] == stages
+                    if list_after >= 0:
+                        assert launch["list_after_step"] == list_after
+                    kernels.add((launch["kernel"], launch["rows_per_lane"], launch["list_after_step"]))
+                    what = f"{rows} rows, {stages} stages, staged {staged}, list after {list_after}"
+                    np.testing.assert_array_equal(got[0], gk, err_msg=what)
+                    np.testing.assert_array_equal(got[1], gs, err_msg=what)
     eng.pin_launch()
+    eng.pin_list_after()
+    kernels_rows = {(k, r) for k, r, _ in kernels}
     if case["config"] in (0, 1, 2) and not case["unfiltered_customer"]:
-        assert ("compiled plan", 4) in kernels and ("compiled plan", 8) in kernels, kernels
-    assert ("interpreted", 4) in kernels
+        assert ("compiled plan", 4) in kernels_rows and ("compiled plan", 8) in kernels_rows, kernels
+    if name in ("c0_small", "c2_small"):
+        assert ("compiled plan", 8, 0) in kernels, kernels  # the row-list form ran
+    assert ("interpreted", 4) in kernels_rows
 
 
 def test_tuned_launch_equals_the_fixed_rule(engine_factory):
