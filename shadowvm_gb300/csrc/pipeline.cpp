@@ -1212,6 +1212,8 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
   configure(pick);
   size_t smem = smem_of(pick);
   int grid = grid_of(pick, smem);
+  const int resident = pick.rows ? star_plan_blocks_per_sm(P, pick.rows, pick.minb, pick.list, smem)
+                                 : star_blocks_per_sm(P, smem);
   {
     std::string steps;
     for (int k = 0; k < P.nsteps; k++) {
@@ -1224,6 +1226,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
     x->last_launch = std::string("{\"kernel\": \"") + (pick.rows ? "compiled plan" : "interpreted") +
                      "\", \"rows_per_lane\": " + std::to_string(pick.rows ? pick.rows : 4) +
                      ", \"blocks_per_sm_compiled_for\": " + std::to_string(pick.minb ? pick.minb : 3) +
+                     ", \"blocks_per_sm\": " + std::to_string(resident) +
                      ", \"list_after_step\": " + std::to_string(pick.rows ? pick.list : 3) +
                      ", \"ring_stages\": " + std::to_string(pick.nst) + ", \"tables_staged\": " +
                      (pick.staged ? "true" : "false") + ", \"steps\": \"" + steps + "\", \"grid\": " +

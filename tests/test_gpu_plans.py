@@ -93,6 +93,28 @@ def test_tuned_launch_equals_the_fixed_rule(engine_factory):
         eng.close()
 
 
+def test_star_join_list_form_keeps_three_blocks_per_sm(engine_factory):
+    """The star join's compiled row-list form (8 rows per lane, 8-bit kept
+    entries, tables probed in L2) stays small enough in registers and
+    shared memory for three resident blocks per SM, and equals the golden
+    rows.  A change that grows the kernel past that loses a third of its
+    warps and shows here before it shows in a bench."""
+    case = GOLDEN["c2_small"]
+    w = W.make(case["config"], **case["kwargs"])
+    gk, gs = golden_rows(case, w.key_num)
+    eng = engine_factory(tuple_per_bulk=w.tuple_per_bulk, autotune=False)
+    W.load_engine(eng, w)
+    eng.pin_launch(8, 2, 0, blocks_per_sm=2)
+    eng.pin_list_after(0)
+    k, s = W.run_engine(eng, w)
+    np.testing.assert_array_equal(k, gk)
+    np.testing.assert_array_equal(s, gs)
+    launch = eng.last_launch()
+    assert launch["kernel"] == "compiled plan" and launch["list_after_step"] == 0, launch
+    assert launch["blocks_per_sm"] >= 3, launch
+    eng.close()
+
+
 def test_query_mix_compiled_equals_interpreted(engine_factory):
     """Every query of the batched mix run alone: the compiled kernel (its
     shapes include a price range in each place the planner puts it) and the
