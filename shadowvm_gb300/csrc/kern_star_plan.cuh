@@ -257,6 +257,16 @@ __device__ __forceinline__ int plan_list_step(const Step& st, const int32_t* wst
 
 // kC: the step after which the warp's live rows become a list (0..2: the
 // later steps run over the list; 3: every step runs over all the warp's rows).
+// Copies a probe step's kept entry of `row` into the next buffered word when
+// the step's entries carry a payload (the host puts those words first, in
+// step order, so `k` is a compile-time index here).
+template <int kCode, int kR, typename PwT>
+__device__ __forceinline__ void append_entry(const Step& st, const PlanList<kR, PwT>& L, int row, uint32_t* ent,
+                                             int& k) {
+  using C = StepCode<kCode>;
+  if (C::probe && C::bits > 1) ent[k++] = (uint32_t)L.pw(st.dim)[row];
+}
+
 template <int kAgg, int kR, int kMinB, int kC, int S0, int S1, int S2, int S3>
 __global__ void __launch_bounds__(kStarThreads, kMinB) star_plan_kernel(const __grid_constant__ StarParams P) {
   using PwT = typename PlanEntryWord<S0, S1, S2, S3>::type;
@@ -386,7 +396,12 @@ __global__ void __launch_bounds__(kStarThreads, kMinB) star_plan_kernel(const __
         if (lane < take) {
           const int row = L.row[done + lane];
           uint32_t* ent = buf + (size_t)(cnt + lane) * W;
-          for (int k = 0; k < W; k++) {
+          int k = 0;
+          append_entry<S0, kR, PwT>(P.steps[0], L, row, ent, k);
+          append_entry<S1, kR, PwT>(P.steps[1], L, row, ent, k);
+          append_entry<S2, kR, PwT>(P.steps[2], L, row, ent, k);
+          append_entry<S3, kR, PwT>(P.steps[3], L, row, ent, k);
+          for (; k < W; k++) {
             const int code = P.agg_src[k];
             ent[k] = code < 8               ? (uint32_t)L.pw(code)[row]
                      : code == kAggRowWord ? (uint32_t)(base + row)

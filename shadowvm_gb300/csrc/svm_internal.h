@@ -403,9 +403,19 @@ inline void flatten_plan(StarParams& P) {
     M.xa = make_extract(P, M.a, 0);
     if (M.form != MF_OPND) M.xb = make_extract(P, M.b, 0);
   }
-  // The buffered row's words: each distinct dim or fact slot an extractor reads.
+  // The buffered row's words: first the table entry of every probe step
+  // whose entries carry a payload, in step order (the compiled kernel copies
+  // these with compile-time word indices), then each further dim or fact
+  // slot an extractor reads.
   P.agg_words = 0;
   if (prog) return;
+  for (int s = 0; s < P.nsteps; s++) {
+    const Step& st = P.steps[s];
+    if (st.kind != STEP_PROBE || st.entry_bits <= 1) continue;
+    int k = 0;
+    while (k < P.agg_words && P.agg_src[k] != st.dim) k++;
+    if (k == P.agg_words) P.agg_src[P.agg_words++] = (int8_t)st.dim;
+  }
   auto word_of = [&](Extract x) {
     const int8_t code = (int8_t)(x.dim >= 0 ? x.dim : x.dim == -2 ? kAggRowWord : 8 + x.slot);
     int k = 0;
