@@ -322,9 +322,11 @@ svm_status svm_pin_launch(svm_ctx* ctx, int rows_per_lane, int blocks_per_sm, in
 
 /* Narrows, in the same way, the compiled kernel's row-list form:
  * list_after -1 (any), 0..2 (after that filter step each warp's live rows
- * become a list and the later steps run over the list only) or 3 (every
- * step runs over all rows, predicated).  Only some plan shapes have the list
- * forms compiled.  No counterpart in the reference. */
+ * become a list and the later steps run over the list only), 3 (every step
+ * runs over all rows, predicated) or 4 (a list after step 0, then steps 1
+ * and 2 over it in one pass, both lookups in flight together).  Only some
+ * plan shapes have the list forms compiled.  No counterpart in the
+ * reference. */
 svm_status svm_pin_list_after(svm_ctx* ctx, int list_after);
 
 /* The same for the merged batch kernel of svm_run_batch / svm_batch_begin:

@@ -804,7 +804,7 @@ svm_status svm_pin_launch(svm_ctx* c, int rows_per_lane, int blocks_per_sm, int 
 
 svm_status svm_pin_list_after(svm_ctx* c, int list_after) {
   if (!c) return SVM_E_INVALID_ARG;
-  if (list_after < -1 || list_after > 3) return SVM_E_INVALID_ARG;
+  if (list_after < -1 || list_after > 4) return SVM_E_INVALID_ARG;
   Ctx* x = C(c);
   std::lock_guard<std::recursive_mutex> g(x->mu);
   x->pin_list = list_after;

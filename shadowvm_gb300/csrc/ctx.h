@@ -174,7 +174,8 @@ struct Ctx {
     int swap = -1;
     int rows = 0;
     int minb = 0;   // compiled kernel: the blocks per SM it is compiled for
-    int list = 3;   // compiled kernel: the step after which later steps run over a row list (3: none)
+    int list = 3;   // compiled kernel: the step after which later steps run over a row list (3: none;
+                    // 4: after step 0, steps 1 and 2 in one pass)
   };
   // Pinned launch choices (svm_pin_launch): kernel rows per lane (-1: any,
   // 0: the interpreted kernel, 4 or 8: the compiled one), the blocks per SM

@@ -256,7 +256,88 @@ __device__ __forceinline__ int plan_list_step(const Step& st, const int32_t* wst
 }
 
 // kC: the step after which the warp's live rows become a list (0..2: the
-// later steps run over the list; 3: every step runs over all the warp's rows).
+// later steps run over the list; 3: every step runs over all the warp's
+// rows; 4: a list after step 0, then steps 1 and 2 over it in one pass).
+// Two compiled filter steps over the warp's list in one pass: each entry's
+// lookups for both steps are issued before either result is used (the
+// second step's table is read for rows the first will drop), so the two
+// probes cost one round trip to L2 instead of two.  Otherwise as
+// plan_list_step.
+template <int kA, int kB, int kR, typename PwT>
+__device__ __forceinline__ int plan_list_step2(const Step& sa, const Step& sb, const int32_t* wstage,
+                                               const uint32_t* tables, const PlanList<kR, PwT>& L, int lane,
+                                               uint32_t lt, int n) {
+  using A = StepCode<kA>;
+  using Bc = StepCode<kB>;
+  if (n == 0) return 0;
+  constexpr int kTR = kConsumerWarps * plan_warp_rows(kR);
+  constexpr int kU = 4;
+  const int32_t* ca = wstage + sa.col * kTR;
+  const int32_t* cb = wstage + sb.col * kTR;
+  int out = 0;
+  for (int r0 = 0; r0 < n; r0 += 32 * kU) {
+    int row[kU];
+    bool live[kU];
+    uint32_t wa[kU], sha[kU], wb[kU], shb[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int i = r0 + u * 32 + lane;
+      live[u] = i < n;
+      row[u] = live[u] ? (int)L.row[i] : 0;
+      const uint32_t ka = (uint32_t)ca[row[u]], kb = (uint32_t)cb[row[u]];
+      bool la = live[u], lb = live[u];
+      if (A::kind == SC_RANGE || A::ranged) la = la && ka - (uint32_t)sa.lo <= (uint32_t)sa.hi - (uint32_t)sa.lo;
+      if (Bc::kind == SC_RANGE || Bc::ranged) lb = lb && kb - (uint32_t)sb.lo <= (uint32_t)sb.hi - (uint32_t)sb.lo;
+      wa[u] = 0u;
+      sha[u] = 0u;
+      wb[u] = 0u;
+      shb[u] = 0u;
+      if (A::probe) {
+        const uint32_t idx = ka - (uint32_t)sa.key_min;
+        la = la && idx < sa.span;
+        const uint32_t bit = idx << A::bits_log2;
+        sha[u] = bit & 31u;
+        if (A::kind == SC_SMEM)
+          wa[u] = la ? tables[sa.smem_word_off + (bit >> 5)] : 0u;
+        else
+          wa[u] = la ? __ldg(sa.words + (bit >> 5)) : 0u;
+      }
+      if (Bc::probe) {
+        const uint32_t idx = kb - (uint32_t)sb.key_min;
+        lb = lb && idx < sb.span;
+        const uint32_t bit = idx << Bc::bits_log2;
+        shb[u] = bit & 31u;
+        if (Bc::kind == SC_SMEM)
+          wb[u] = lb ? tables[sb.smem_word_off + (bit >> 5)] : 0u;
+        else
+          wb[u] = lb ? __ldg(sb.words + (bit >> 5)) : 0u;
+      }
+      live[u] = la && lb;
+    }
+    uint32_t ea[kU], eb[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      ea[u] = A::bits == 32 ? wa[u] : (wa[u] >> sha[u]) & ((1u << (A::bits & 31)) - 1u);
+      eb[u] = Bc::bits == 32 ? wb[u] : (wb[u] >> shb[u]) & ((1u << (Bc::bits & 31)) - 1u);
+      if (A::probe) live[u] = live[u] && (ea[u] & 1u);
+      if (Bc::probe) live[u] = live[u] && (eb[u] & 1u);
+    }
+    __syncwarp();  // every entry of this round is read before any is overwritten
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const uint32_t b = __ballot_sync(0xffffffffu, live[u]);
+      if (live[u]) {
+        L.row[out + __popc(b & lt)] = (uint16_t)row[u];
+        if (A::probe && A::bits > 1) L.pw(sa.dim)[row[u]] = (PwT)ea[u];
+        if (Bc::probe && Bc::bits > 1) L.pw(sb.dim)[row[u]] = (PwT)eb[u];
+      }
+      out += __popc(b);
+    }
+    __syncwarp();
+  }
+  return out;
+}
+
 // Copies a probe step's kept entry of `row` into the next buffered word when
 // the step's entries carry a payload (the host puts those words first, in
 // step order, so `k` is a compile-time index here).
@@ -366,29 +447,34 @@ __global__ void __launch_bounds__(kStarThreads, kMinB) star_plan_kernel(const __
       }
       int n = 0;
       plan_step_if<S0, kR, PwT>(P.steps[0], wstage, tables, L, lane, mask);
-      if (kC == 0) n = plan_sorted_list<kR, PwT>(L, lane, lt, mask);
-      if (kC < 1)
-        n = plan_list_step<S1, kR, PwT>(P.steps[1], wstage, tables, L, lane, lt, n);
-      else
-        plan_step_if<S1, kR, PwT>(P.steps[1], wstage, tables, L, lane, mask);
-      if (kC == 1) n = plan_sorted_list<kR, PwT>(L, lane, lt, mask);
-      if (kC < 2)
-        n = plan_list_step<S2, kR, PwT>(P.steps[2], wstage, tables, L, lane, lt, n);
-      else
-        plan_step_if<S2, kR, PwT>(P.steps[2], wstage, tables, L, lane, mask);
-      if (kC == 2) n = plan_sorted_list<kR, PwT>(L, lane, lt, mask);
-      if (kC < 3) {
+      if (kC == 0 || kC == 4) n = plan_sorted_list<kR, PwT>(L, lane, lt, mask);
+      if (kC == 4) {
+        n = plan_list_step2<S1, S2, kR, PwT>(P.steps[1], P.steps[2], wstage, tables, L, lane, lt, n);
         n = plan_list_step<S3, kR, PwT>(P.steps[3], wstage, tables, L, lane, lt, n);
       } else {
-        plan_step_if<S3, kR, PwT>(P.steps[3], wstage, tables, L, lane, mask);
-        // ---- the survivors as a list of row offsets
+        if (kC < 1)
+          n = plan_list_step<S1, kR, PwT>(P.steps[1], wstage, tables, L, lane, lt, n);
+        else
+          plan_step_if<S1, kR, PwT>(P.steps[1], wstage, tables, L, lane, mask);
+        if (kC == 1) n = plan_sorted_list<kR, PwT>(L, lane, lt, mask);
+        if (kC < 2)
+          n = plan_list_step<S2, kR, PwT>(P.steps[2], wstage, tables, L, lane, lt, n);
+        else
+          plan_step_if<S2, kR, PwT>(P.steps[2], wstage, tables, L, lane, mask);
+        if (kC == 2) n = plan_sorted_list<kR, PwT>(L, lane, lt, mask);
+        if (kC < 3) {
+          n = plan_list_step<S3, kR, PwT>(P.steps[3], wstage, tables, L, lane, lt, n);
+        } else {
+          plan_step_if<S3, kR, PwT>(P.steps[3], wstage, tables, L, lane, mask);
+          // ---- the survivors as a list of row offsets
 #pragma unroll
-        for (int j = 0; j < kR; j++) {
-          const uint32_t b = __ballot_sync(0xffffffffu, (mask >> j) & 1u);
-          if ((mask >> j) & 1u) L.row[n + __popc(b & lt)] = (uint16_t)plan_row<kR>(lane, j);
-          n += __popc(b);
+          for (int j = 0; j < kR; j++) {
+            const uint32_t b = __ballot_sync(0xffffffffu, (mask >> j) & 1u);
+            if ((mask >> j) & 1u) L.row[n + __popc(b & lt)] = (uint16_t)plan_row<kR>(lane, j);
+            n += __popc(b);
+          }
+          __syncwarp();
         }
-        __syncwarp();
       }
       // ---- their operand words into the warp's buffer, aggregated 32 rows at a time
       for (int done = 0; done < n;) {

@@ -21,11 +21,16 @@ extern const PlanEntry kPlansList[] = {
     // date + part join with the part presence prefilter first
     SVM_PLAN_LIST(AGG_DENSE_SMEM, 0, l2(0), l2(2), l2(3), SC_NONE),
     SVM_PLAN_LIST(AGG_DENSE_SMEM, 0, l2(0), smem(2), l2(3), SC_NONE),
+    SVM_PLAN_LIST(AGG_DENSE_SMEM, 4, l2(0), l2(2), l2(3), SC_NONE),
+    SVM_PLAN_LIST(AGG_DENSE_SMEM, 4, l2(0), smem(2), l2(3), SC_NONE),
     // the star join: date, customer, supplier
     SVM_PLAN_LIST(AGG_DENSE_SMEM, 0, l2(2), l2(2), l2(2), SC_NONE),
     SVM_PLAN_LIST(AGG_DENSE_SMEM, 1, l2(2), l2(2), l2(2), SC_NONE),
     SVM_PLAN_LIST(AGG_DENSE_SMEM, 0, smem(2), l2(2), l2(2), SC_NONE),
     SVM_PLAN_LIST(AGG_DENSE_SMEM, 1, smem(2), l2(2), l2(2), SC_NONE),
+    // the star join with the customer and supplier probes in one pass
+    SVM_PLAN_LIST(AGG_DENSE_SMEM, 4, l2(2), l2(2), l2(2), SC_NONE),
+    SVM_PLAN_LIST(AGG_DENSE_SMEM, 4, smem(2), l2(2), l2(2), SC_NONE),
 };
 extern const int kPlansListCount = (int)(sizeof(kPlansList) / sizeof(kPlansList[0]));
 

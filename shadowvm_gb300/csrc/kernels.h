@@ -94,7 +94,8 @@ size_t star_smem_bytes(const StarParams& p);
 // and an instantiated shape; rows_per_lane 4 (for 3 or 4 blocks per SM) or
 // 8 (for 2 blocks per SM), min_blocks the blocks per SM it is compiled for,
 // list_after the step after which the later steps run over a list of the
-// warp's live rows (3: none do).
+// warp's live rows (3: none do; 4: after step 0, with steps 1 and 2 in one
+// pass over the list).
 int star_plan_code(const StarParams& p, int k);  // step k's code (-1: not compilable)
 bool star_plan_available(const StarParams& p, int rows_per_lane, int min_blocks, int list_after);
 size_t star_plan_smem_bytes(const StarParams& p, int rows_per_lane);

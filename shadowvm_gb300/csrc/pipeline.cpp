@@ -1138,7 +1138,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
     for (int staged = 1; staged >= (any_staged ? 0 : 1); staged--)
       for (const auto& rm : {std::make_pair(4, 3), std::make_pair(4, 4), std::make_pair(8, 2), std::make_pair(0, 0)})
         for (int nst = kStages; nst >= 2; nst--)
-          for (int la = 3; la >= 0; la--) {
+          for (int la = 4; la >= 0; la--) {
             const int rows = rm.first;
             if ((x->pin_rows >= 0 && rows != x->pin_rows) || (x->pin_stages && nst != x->pin_stages) ||
                 (x->pin_staged >= 0 && staged != x->pin_staged) || (x->pin_minb && rm.second != x->pin_minb) ||
@@ -1165,8 +1165,8 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
                                           ? "no launch configuration of this plan fits the pinned choices"
                                           : "shared-memory plan too large");
   auto rule_rank = [](const Fit& f) {  // larger is preferred
-    return (f.c.rows == 4 ? 2 : f.c.rows == 8 ? 1 : 0) * 10000000 + f.c.list * 1000000 + f.blocks * 1000 +
-           f.c.nst * 10 + (f.c.staged ? 1 : 0);
+    return (f.c.rows == 4 ? 2 : f.c.rows == 8 ? 1 : 0) * 10000000 + (f.c.list == 3 ? 1000000 : 0) +
+           f.blocks * 1000 + f.c.nst * 10 + (f.c.staged ? 1 : 0);
   };
   Cand pick = cands[0].c;
   int best_rank = -1;

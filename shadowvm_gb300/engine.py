@@ -247,7 +247,8 @@ class Engine:
     def pin_list_after(self, list_after: int = -1):
         """Narrows the compiled scan's row-list form (svm_pin_list_after):
         -1 any, 0..2 the step after which later steps run over a list of
-        the live rows, 3 none."""
+        the live rows, 3 none, 4 a list after step 0 with steps 1 and 2
+        over it in one pass."""
         self._check(self.lib.svm_pin_list_after(self.h, list_after))
 
     def pin_batch_launch(self, consumer_warps: int = 0, ring_stages: int = 0):

@@ -46,7 +46,7 @@ def test_every_launch_variant_equals_the_reference(engine_factory, name):
     for rows, minb in ((4, 3), (4, 4), (8, 2), (0, 0)):
         for stages in (2, 3):
             for staged in (1, 0):
-                for list_after in ((3, 0, 1) if rows == 8 else (-1,)):
+                for list_after in ((3, 0, 1, 4) if rows == 8 else (-1,)):
                     eng.pin_launch(rows, stages, staged, blocks_per_sm=minb)
                     eng.pin_list_after(list_after)
                     try:
