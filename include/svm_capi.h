@@ -233,7 +233,9 @@ svm_status svm_run_batch(svm_ctx* ctx, int n, const svm_pipeline* pipes);
  * pipeline in input order, each column's rows from an 8-byte-aligned
  * offset) and frees the fold; every fold must be released, also one whose
  * wait failed.  The objects a fold reads must not be replaced until its
- * wait returns. */
+ * wait returns.  A fold never times launch configurations (with autotune,
+ * svm_run_batch does, the first time it meets a batch shape): it takes the
+ * one cached for its batch shape, else the rule. */
 typedef struct svm_fold svm_fold;
 svm_status svm_batch_begin(svm_ctx* ctx, int n, const svm_pipeline* pipes, int host_results, svm_fold** out);
 svm_status svm_batch_wait(svm_ctx* ctx, svm_fold* fold, unsigned long long* nrows_out, unsigned long long* needed);

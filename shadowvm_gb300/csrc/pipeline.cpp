@@ -2065,8 +2065,13 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items, FoldPart* async_par
       // split (28 + 4 or 24 + 8) and the ring depth (at most the rule's,
       // which fits every descriptor of the launch).  The rule: 28 + 4, the
       // deepest ring.  With autotuning, the first launch of a batch shape
-      // times every candidate on the batch itself (slots and tile counters
-      // zeroed before each and again after), and the fastest is kept.
+      // times every candidate on the batch itself (this launch's slots and
+      // tile counter zeroed before each and again after -- only this
+      // launch's: the fold's earlier launches have already written theirs),
+      // and the fastest is kept.  A fold begun without waiting never times
+      // candidates (that would wait for the device inside svm_batch_begin and
+      // hold up the folds behind it): it takes the choice cached for its
+      // batch shape, else the rule.
       std::vector<std::pair<int, int>> cands;  // (consumer warps, ring stages)
       for (int cw : {28, 24})
         for (int nst = mst; nst >= 2; nst--)
@@ -2083,7 +2088,14 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items, FoldPart* async_par
         auto hit = x->batch_tune.find(key);
         if (hit != x->batch_tune.end()) {
           pick = hit->second;
-        } else {
+          tuned = true;
+        } else if (!async_part) {
+          // This launch's queries own one contiguous run of slots.
+          const BatchQuery& ql = dqs[q0 + qn - 1];
+          const unsigned long long s_lo = dqs[q0].slot_off;
+          const unsigned long long s_hi = ql.slot_off + (unsigned long long)(ql.nmetrics + 1) * ql.ngroups;
+          unsigned long long* part_slots = (unsigned long long*)slots + s_lo;
+          const size_t part_bytes = 8 * (size_t)(s_hi - s_lo);
           cudaEvent_t t0, t1;
           cudaEventCreate(&t0);
           cudaEventCreate(&t1);
@@ -2094,8 +2106,8 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items, FoldPart* async_par
             const size_t sm = mbatch_smem_bytes(B);
             const int g = mbatch_grid_size(B, sm);
             if (g <= 0) continue;
-            if (!e) e = cudaMemsetAsync(slots, 0, 8 * slot_words, x->stream);
-            if (!e) e = cudaMemsetAsync(ctr, 0, 8 * (nlaunch + 1), x->stream);
+            if (!e) e = cudaMemsetAsync(part_slots, 0, part_bytes, x->stream);
+            if (!e) e = cudaMemsetAsync(B.tile_counter, 0, 8, x->stream);
             if (!e) e = cudaEventRecord(t0, x->stream);
             if (!e) e = launch_mbatch(B, g, sm, x->stream);
             if (!e) e = cudaEventRecord(t1, x->stream);
@@ -2110,12 +2122,12 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items, FoldPart* async_par
           }
           cudaEventDestroy(t0);
           cudaEventDestroy(t1);
-          if (!e) e = cudaMemsetAsync(slots, 0, 8 * slot_words, x->stream);
-          if (!e) e = cudaMemsetAsync(ctr, 0, 8 * (nlaunch + 1), x->stream);
+          if (!e) e = cudaMemsetAsync(part_slots, 0, part_bytes, x->stream);
+          if (!e) e = cudaMemsetAsync(B.tile_counter, 0, 8, x->stream);
           if (e) return x->cuda_fail(e, "batch kernel tuning");
           x->batch_tune[key] = pick;
+          tuned = true;
         }
-        tuned = true;
       }
       B.cwarps = pick.first;
       B.nstages = pick.second;

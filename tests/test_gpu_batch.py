@@ -139,6 +139,23 @@ def test_batch_larger_than_one_launch(engine_factory):
         np.testing.assert_array_equal(many[i][1], one[i][1], err_msg=f"sums of query {i}")
 
 
+def test_batch_tuned_on_first_use_over_several_launches(engine_factory):
+    """A batch split over several merged launches whose later launch meets a
+    new batch shape (another query-count class, so the launch tuner times
+    its candidates on it) keeps what the earlier launches wrote: every
+    query equals its run alone."""
+    bw = W.make_batch(520, qseed=31, **SMALL)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, batch_policy="always", autotune=True)
+    W.load_batch(eng, bw)
+    one = singles(eng, bw)
+    many = batched(eng, bw)
+    launch = eng.last_launch()
+    assert launch["kernel"] == "batch" and launch["merged_launches"] >= 2 and launch["tuned"], launch
+    for i in range(len(bw.queries)):
+        np.testing.assert_array_equal(many[i][0], one[i][0], err_msg=f"keys of query {i}")
+        np.testing.assert_array_equal(many[i][1], one[i][1], err_msg=f"sums of query {i}")
+
+
 def test_served_loop_results_equal_alone(engine_factory):
     """Requests arriving from several threads are folded into batched
     launches by the served loop; each result equals the query run alone."""

@@ -62,6 +62,29 @@ def test_two_folds_in_flight_equal_single_launches(engine_factory):
             np.testing.assert_array_equal(os_, alone[i][1])
 
 
+def test_fold_takes_the_cached_or_rule_launch(engine_factory):
+    """A fold never times launch configurations: on a fresh context it runs
+    the rule's (reported untuned), after svm_run_batch has tuned the same
+    batch shape it takes that choice; both give the queries' own results."""
+    bw = W.make_batch(40, qseed=37, **SMALL)
+    eng = engine_factory(tuple_per_bulk=bw.fact.tuple_per_bulk, batch_policy="always", autotune=True)
+    W.load_batch(eng, bw)
+    alone = singles(eng, bw, range(40))
+    for round_, tuned in ((0, False), (1, True)):
+        if tuned:
+            eng.run_batch([renamed(q, f"warm{i}") for i, q in enumerate(bw.queries)])
+        pipes = [renamed(q, f"f{round_}_{i}") for i, q in enumerate(bw.queries)]
+        f = eng.batch_begin(pipes, host_results=False)
+        f.wait()
+        f.release()
+        launch = eng.last_launch()
+        assert launch["kernel"] == "batch" and launch["tuned"] == tuned, launch
+        for i, p in enumerate(pipes):
+            k, v = eng.result(p.id, bw.queries[i].key_num)
+            np.testing.assert_array_equal(k, alone[i][0], err_msg=f"keys of query {i}")
+            np.testing.assert_array_equal(v, alone[i][1], err_msg=f"sums of query {i}")
+
+
 def test_fold_with_maps_unbatchable_and_empty(engine_factory):
     """Map pipelines and reduce pipelines the batch kernel does not take
     complete inside begin; their results come back with the fold's."""
