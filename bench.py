@@ -391,10 +391,19 @@ def ours_arm(args):
         qp = copy.deepcopy(w.query)
         qp.pre_pipeline_id[0] = "lineorder_e2e"
         cols = [pinned[c][1] if c in pinned else None for c in range(len(w.fact_cols))]
+
+        def max_over_ranks(v):
+            if world > 1:
+                import torch.distributed as dist
+                t = torch.tensor([v], device="cuda")
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                v = float(t.item())
+            return v
+
+        # (1) every column uploaded each step (svm_object_put), then the query
         eng.put("lineorder_e2e", cols)
         eng.run(qp)
         barrier()
-        h2d = sum(4 * rows for _ in used)
         times = []
         for _ in range(max(1, min(args.steps, 10))):
             t0 = time.perf_counter()
@@ -402,19 +411,45 @@ def ours_arm(args):
             eng.run(qp)
             keys, sums = eng.result(qp.id, w.key_num)
             times.append(time.perf_counter() - t0)
+        copy_s = max_over_ranks(statistics.median(times))
+        copy_h2d = sum(4 * rows for _ in used)
+        eng.drop("lineorder_e2e")
+        # (2) the headline: the columns left in page-locked host memory and read
+        # in place (svm_object_put_host, as the reference keeps its fact bulks in
+        # mapped pinned memory): the scan copies the columns its filters read
+        # and gathers the others from host memory at the surviving rows
+        qh = copy.deepcopy(w.query)
+        qh.pre_pipeline_id[0] = "lineorder_e2h"
+        eng.put_host("lineorder_e2h", cols)
+        eng.run(qh)
+        barrier()
+        times = []
+        for _ in range(max(1, min(args.steps, 10))):
+            t0 = time.perf_counter()
+            eng.put_host("lineorder_e2h", cols)
+            eng.run(qh)
+            keys, sums = eng.result(qh.id, w.key_num)
+            times.append(time.perf_counter() - t0)
+        hl = eng.last_launch()
+        e2e_s = max_over_ranks(statistics.median(times))
+        staged, late = int(hl.get("staged_columns", len(used))), int(hl.get("late_columns", 0))
+        h2d = 4 * rows * staged
         d2h = keys.nbytes + sums.nbytes
-        e2e_s = statistics.median(times)
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([e2e_s], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
         e2e = {"value": rows * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
                "h2d_gb_per_s": h2d / e2e_s / 1e9,
+               "h2d_note": f"{staged} columns the filters read copied per step ({h2d} B); {late} metric "
+                           "column(s) read from host memory only at the surviving rows (4 B per row, fetched "
+                           "in 32 B sectors; not counted)",
                "host_numa": {"gpu_node": node, "pinned_pages_on_node": {str(k): v for k, v in placed.items()}},
-               "api": "svm_object_put (pinned host columns) + svm_run_pipeline + svm_object_read"}
-        eng.drop("lineorder_e2e")
+               "api": "svm_object_put_host (page-locked host columns, read in place) + svm_run_pipeline + "
+                      "svm_object_read",
+               "copy_all": {"value": rows * world / copy_s, "unit": UNIT, "ms_per_step": copy_s * 1e3,
+                            "h2d_bytes_per_step": copy_h2d, "h2d_gb_per_s": copy_h2d / copy_s / 1e9,
+                            "api": "svm_object_put (every column uploaded) + svm_run_pipeline + "
+                                   "svm_object_read"}}
+        eng.drop(qh.id)
+        eng.drop("lineorder_e2h")
 
     cpu, parity = None, None
     if rank == 0 and not args.no_cpu_baseline:

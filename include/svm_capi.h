@@ -115,6 +115,19 @@ typedef struct svm_column_desc { /* ColumnInfo (svm.proto:73-79) */
 svm_status svm_object_put(svm_ctx* ctx, const char* id, int ncols, const int* types,
                           unsigned long long nrows, const void* const* columns,
                           int columns_on_device);
+/* A fact table left in the caller's page-locked host memory (cudaHostAlloc /
+ * cudaHostRegister; anything else is SVM_E_INVALID_ARG), Int32 / Int64
+ * columns, read in place: the reference keeps its fact bulks in mapped
+ * pinned host memory too (object/object.cpp:194-294, SharedMem).  A reduce
+ * pipeline's scan copies to the device only the rows and columns its filter
+ * steps read, and gathers the other columns it needs from host memory at the
+ * rows that survive.  The buffers must stay valid and unchanged while the
+ * object exists.  Only a reduce pipeline's source may be such an object
+ * (run alone, not batched); joins, Map pipelines, reads, generation and
+ * device pointers of it are SVM_E_UNSUPPORTED.  A NULL column is absent (a
+ * pipeline that reads it fails). */
+svm_status svm_object_put_host(svm_ctx* ctx, const char* id, int ncols, const int* types,
+                               unsigned long long nrows, const void* const* columns);
 /* As svm_object_put, with each column described by {type, val_size}:
  * SVM_INT32 / SVM_INT64 as above, or SVM_STRING of val_size bytes per value
  * (the reference's fixed-width char[val_size] String column, com/svm.proto:

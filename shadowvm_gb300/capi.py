@@ -98,6 +98,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "svm_stream": (P, [P]),
         "svm_bytes_in_use": (U64, [P]),
         "svm_object_put": (I, [P, cp, I, ctypes.POINTER(I), U64, ctypes.POINTER(P), I]),
+        "svm_object_put_host": (I, [P, cp, I, ctypes.POINTER(I), U64, ctypes.POINTER(P)]),
         "svm_object_put_columns": (I, [P, cp, I, ctypes.POINTER(svm_column_desc), U64, ctypes.POINTER(P), I]),
         "svm_object_columns": (I, [P, cp, ctypes.POINTER(svm_column_desc), I]),
         "svm_object_gen_uniform": (I, [P, cp, I, U64, U64, U64, I, I, ctypes.POINTER(I)]),

@@ -10,7 +10,7 @@
 namespace svm {
 
 DevBuf::~DevBuf() {
-  if (!p) return;
+  if (!p || !owned) return;
   if (ctx)
     ctx->release(p, bytes);
   else
@@ -358,7 +358,7 @@ svm_status svm_object_put_columns(svm_ctx* c, const char* id, int ncols, const s
   }
   // Replacing an object of the same shape that no view shares: reuse its storage.
   ObjectPtr old = x->find(id);
-  bool reuse = old && old->ncols == ncols && old->nrows == nrows && old->row0 == 0 &&
+  bool reuse = old && !old->host && old->ncols == ncols && old->nrows == nrows && old->row0 == 0 &&
                (int)old->storage.size() == ncols;
   for (int k = 0; reuse && k < ncols; k++)
     reuse = old->types[k] == cols[k].type && old->storage[k].use_count() == 1;
@@ -416,6 +416,48 @@ svm_status svm_object_put_columns(svm_ctx* c, const char* id, int ncols, const s
   if (e) return x->cuda_fail(e, "object upload");
   x->put_object(id, o);
   x->purge_rank_cache();
+  return SVM_OK;
+}
+
+svm_status svm_object_put_host(svm_ctx* c, const char* id, int ncols, const int* types,
+                               unsigned long long nrows, const void* const* columns) {
+  if (!c || !id || ncols <= 0 || ncols > 64 || !types || !columns) return SVM_E_INVALID_ARG;
+  Ctx* x = C(c);
+  std::lock_guard<std::recursive_mutex> g(x->mu);
+  cudaSetDevice(x->device);
+  x->err.clear();
+  auto o = std::make_shared<svm::Object>();
+  o->id = id;
+  o->version = x->next_version++;
+  o->ncols = ncols;
+  o->nrows = nrows;
+  o->host = true;
+  o->has_bulks = nrows > 0;
+  o->bulk0_rows = nrows < x->cfg.tuple_per_bulk ? nrows : x->cfg.tuple_per_bulk;
+  o->source_rows = nrows;
+  for (int k = 0; k < ncols; k++) {
+    const int t = types[k];
+    if (t != SVM_INT32 && t != SVM_INT64)
+      return x->fail(SVM_E_UNSUPPORTED, "host-resident object columns must be Int32 or Int64");
+    const size_t el = t == SVM_INT64 ? 8 : 4;
+    if (columns[k] && nrows) {
+      if ((uintptr_t)columns[k] % el)
+        return x->fail(SVM_E_INVALID_ARG, "column " + std::to_string(k) + " is not aligned to its element size");
+      cudaPointerAttributes a{};
+      if (cudaPointerGetAttributes(&a, columns[k]) != cudaSuccess || a.type != cudaMemoryTypeHost) {
+        cudaGetLastError();
+        return x->fail(SVM_E_INVALID_ARG,
+                       "column " + std::to_string(k) + " is not page-locked host memory (cudaHostAlloc / cudaHostRegister)");
+      }
+    }
+    auto b = std::make_shared<svm::DevBuf>();
+    b->p = const_cast<void*>(columns[k]);
+    b->bytes = columns[k] ? nrows * el : 0;
+    b->owned = false;
+    o->types.push_back(t);
+    o->storage.push_back(b);
+  }
+  x->put_object(id, o);
   return SVM_OK;
 }
 
@@ -516,6 +558,7 @@ svm_status svm_object_gen_uniform(svm_ctx* c, const char* id, int col, unsigned 
   cudaSetDevice(x->device);
   ObjectPtr o = x->find(id);
   if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
+  if (o->host) return x->fail(SVM_E_UNSUPPORTED, "gen_uniform: object " + std::string(id) + " lives in host memory");
   if (col < 0 || col >= o->ncols || o->types[col] != SVM_INT32)
     return x->fail(SVM_E_INVALID_ARG, "gen_uniform needs an int32 column");
   svm::DevBufPtr lut;
@@ -588,6 +631,7 @@ svm_status svm_object_read(svm_ctx* c, const char* id, int col, unsigned long lo
   cudaSetDevice(x->device);
   ObjectPtr o = x->find(id);
   if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
+  if (o->host) return x->fail(SVM_E_UNSUPPORTED, "object " + std::string(id) + " lives in host memory (svm_object_put_host): read it in place");
   if (col < 0 || col >= o->ncols || row0 > o->nrows || n > o->nrows - row0)
     return x->fail(SVM_E_INVALID_ARG, "read out of range");
   if (!n) return SVM_OK;
@@ -634,6 +678,7 @@ svm_status svm_object_device_ptr(svm_ctx* c, const char* id, int col, void** dpt
   std::lock_guard<std::recursive_mutex> g(x->mu);
   ObjectPtr o = x->find(id);
   if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + id);
+  if (o->host) return x->fail(SVM_E_UNSUPPORTED, "object " + std::string(id) + " lives in host memory (svm_object_put_host): read it in place");
   if (col < 0 || col >= o->ncols) return x->fail(SVM_E_INVALID_ARG, "bad column");
   *dptr = o->col(col);
   return SVM_OK;
@@ -685,6 +730,8 @@ svm_status svm_objects_read(svm_ctx* c, int n, const char* const* ids, void* hos
   for (int k = 0; k < n; k++) {
     ObjectPtr o = ids[k] ? x->find(ids[k]) : nullptr;
     if (!o) return x->fail(SVM_E_NOT_FOUND, std::string("no object ") + (ids[k] ? ids[k] : "(null)"));
+    if (o->host)
+      return x->fail(SVM_E_UNSUPPORTED, "object " + std::string(ids[k]) + " lives in host memory (svm_object_put_host)");
     nrows_out[k] = o->nrows;
     for (int col = 0; col < o->ncols; col++) {
       if (o->is_string(col))

@@ -24,6 +24,7 @@ struct DevBuf {
   Ctx* ctx = nullptr;
   void* p = nullptr;
   size_t bytes = 0;
+  bool owned = true;  // false: p is the caller's memory (a host-resident object's column)
   ~DevBuf();
 };
 using DevBufPtr = std::shared_ptr<DevBuf>;
@@ -68,6 +69,11 @@ struct Object {
   unsigned long long nrows = 0;
   unsigned long long row0 = 0;                // rows skipped in the base storage (views)
   std::vector<DevBufPtr> storage;             // base allocation per column
+  // Columns in the caller's page-locked host memory (svm_object_put_host),
+  // read in place: only the fused scan of a reduce pipeline takes such an
+  // object (as its fact table), copying the columns its filters read and
+  // gathering the others at the surviving rows.
+  bool host = false;
   // The reference keeps objects as bulks of tuple_per_bulk rows and joins only
   // against bulk 0 of a joined object (core/pipeline.cu:91,295).
   bool has_bulks = false;

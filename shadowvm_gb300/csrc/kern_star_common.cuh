@@ -35,11 +35,19 @@ __device__ __forceinline__ void smem_add64(unsigned long long* p, unsigned long 
 // ---------------------------------------------------------------- deferred aggregation
 constexpr int kAggCap = 32;  // buffered rows per warp
 
+// A gathered value: a plain global load, since the column may be a
+// host-resident table's late column in page-locked host memory.
+__device__ __forceinline__ int32_t load_gather(const int32_t* p) {
+  int32_t v;
+  asm("ld.global.s32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+
 // An extractor over a buffered row's words (agg_src order).
 __device__ __forceinline__ uint32_t extract_entry(const Extract& x, const uint32_t* ent) {
   if (x.dim < 0) return ent[x.slot] + (uint32_t)x.base;
   uint32_t v = (ent[x.dim] >> x.shift) & x.mask;
-  if (x.col) v = (uint32_t)__ldg(x.col + v);
+  if (x.col) v = (uint32_t)load_gather(x.col + v);
   return v + (uint32_t)x.base;
 }
 

@@ -1103,7 +1103,11 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
                                            : std::string();  // as planned
   // The compiled kernel reads the columns no filter step needs only at the
   // surviving rows (late columns); the interpreted kernel stages them all.
+  // For a host-resident fact table the staged columns are device copies
+  // (host_to_dev) and the late columns stay in host memory.
   const StarParams P0 = P;
+  std::map<const int32_t*, const int32_t*> host_to_dev;
+  bool host_unmapped = false;  // a staged column still points at host memory
   auto configure = [&](const Cand& c) {
     P = P0;
     P.nstages = c.nst;
@@ -1113,12 +1117,22 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
     if (c.swap >= 0) std::swap(P.steps[c.swap], P.steps[c.swap + 1]);
     if (c.rows) apply_late_columns(P);
     flatten_plan(P);
+    host_unmapped = false;
+    if (src->host)
+      for (int k = 0; k < P.ncols; k++) {
+        auto it = host_to_dev.find(P.cols[k]);
+        if (it != host_to_dev.end())
+          P.cols[k] = it->second;
+        else
+          host_unmapped = true;
+      }
   };
   auto smem_of = [&](const Cand& c) { return c.rows ? star_plan_smem_bytes(P, c.rows) : star_smem_bytes(P); };
   auto grid_of = [&](const Cand& c, size_t sm) {
     return c.rows ? star_plan_grid_size(P, c.rows, c.minb, c.list, sm) : star_grid_size(P, sm);
   };
   auto launch = [&](const Cand& c, size_t sm) {
+    if (host_unmapped) return cudaErrorInvalidValue;  // never scan host memory with bulk copies
     return c.rows ? launch_star_plan(P, c.rows, c.minb, c.list, grid_of(c, sm), sm, x->stream)
                   : launch_star(P, grid_of(c, sm), star_block_size(), sm, x->stream);
   };
@@ -1164,6 +1178,43 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
                                               x->pin_list >= 0
                                           ? "no launch configuration of this plan fits the pinned choices"
                                           : "shared-memory plan too large");
+  // A host-resident fact table: every candidate must stage the same columns,
+  // so only compiled kernels run its scan when one fits (they all keep the
+  // same late columns); the staged columns' rows this scan reads are copied
+  // to the device now, the late ones are gathered from host memory.  (The
+  // gathers cross the same host link as the copies, about one transfer per
+  // surviving row; overlapping the copies with the scan in row chunks was
+  // measured and gains nothing: the link's bytes bound both.)
+  std::vector<DevBufPtr> host_copies;
+  if (src->host) {
+    bool any_compiled = false;
+    for (const Fit& f : cands) any_compiled |= f.c.rows != 0;
+    if (any_compiled)
+      cands.erase(std::remove_if(cands.begin(), cands.end(), [](const Fit& f) { return f.c.rows == 0; }),
+                  cands.end());
+    configure(cands[0].c);
+    const long long a0 = P.row_begin & ~3ll, end4 = (P.row_end + 3) & ~3ll;
+    for (int k = 0; k < P.ncols; k++) {
+      const int32_t* h = P.cols[k];
+      if (host_to_dev.count(h)) continue;
+      const DevBuf* hb = nullptr;
+      for (const DevBufPtr& s : src->storage)
+        if (s && s->p == (const void*)h) hb = s.get();
+      if (!h || !hb) return x->fail(SVM_E_INVALID_ARG, "a host-resident column the scan reads has no data");
+      const long long base_rows = (long long)(hb->bytes / 4);
+      const long long hi = std::min(end4, base_rows);
+      DevBufPtr d;
+      if ((st = x->alloc((size_t)(end4 - a0 + 64) * 4, &d))) return st;
+      if (hi > a0 && (e = cudaMemcpyAsync(d->p, h + a0, (size_t)(hi - a0) * 4, cudaMemcpyHostToDevice, x->stream)))
+        return x->cuda_fail(e, "host-resident column copy");
+      host_to_dev[h] = (const int32_t*)d->p - a0;  // indexed by base row, like the host column
+      host_copies.push_back(d);
+    }
+  }
+  auto same_cand = [](const Cand& a, const Cand& z) {
+    return a.nst == z.nst && a.staged == z.staged && a.swap == z.swap && a.rows == z.rows && a.minb == z.minb &&
+           a.list == z.list;
+  };
   auto rule_rank = [](const Fit& f) {  // larger is preferred
     return (f.c.rows == 4 ? 2 : f.c.rows == 8 ? 1 : 0) * 10000000 + (f.c.list == 3 ? 1000000 : 0) +
            f.blocks * 1000 + f.c.nst * 10 + (f.c.staged ? 1 : 0);
@@ -1181,7 +1232,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
     auto hit = x->star_tune.find(key);
     if (hit != x->star_tune.end()) {
       pick = hit->second;
-    } else {
+    } else if (!src->host) {  // a host-resident table takes the cached choice or the rule
       cudaEvent_t t0, t1;
       cudaEventCreate(&t0);
       cudaEventCreate(&t1);
@@ -1207,6 +1258,18 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
       if (e) return x->cuda_fail(e, "star kernel tuning");
       x->star_tune[key] = pick;
       if ((e = cudaMemsetAsync(sums, 0, agg_bytes, x->stream))) return x->cuda_fail(e, "cudaMemsetAsync");
+    }
+  }
+  if (src->host) {  // a choice cached from a device-resident table may not stage the same columns
+    bool ok = false;
+    for (const Fit& f : cands) ok |= same_cand(f.c, pick);
+    if (!ok) {
+      int r = -1;
+      for (const Fit& f : cands)
+        if (rule_rank(f) > r) {
+          r = rule_rank(f);
+          pick = f.c;
+        }
     }
   }
   configure(pick);
@@ -1417,8 +1480,16 @@ svm_status resolve(Ctx* x, const svm_pipeline* p, Bound* b, ObjectPtr* src, std:
     if (!o)
       return x->fail(SVM_E_NOT_FOUND,
                      std::string("no object ") + (p->pre_pipeline_id[i] ? p->pre_pipeline_id[i] : "(null)"));
+    if (o->host)
+      return x->fail(SVM_E_UNSUPPORTED, std::string("joined object ") + p->pre_pipeline_id[i] +
+                                            " lives in host memory (svm_object_put_host): only a reduce "
+                                            "pipeline's fact table may");
     refs->push_back(o);
   }
+  if ((*src)->host && !b->is_reduce)
+    return x->fail(SVM_E_UNSUPPORTED, std::string("object ") + p->pre_pipeline_id[0] +
+                                          " lives in host memory (svm_object_put_host): only a reduce "
+                                          "pipeline scans such an object");
   return resolve_strings(x, b, *src, *refs);
 }
 
@@ -2287,7 +2358,7 @@ svm_status run_batch(Ctx* x, int n, const svm_pipeline* p) {
     it.b = b;
     it.refs = refs;
     if ((st = plan_star_cached(x, b, src, refs, &it.plan))) return st;
-    bool eligible = !it.plan.empty_src && !it.plan.needs_prog;
+    bool eligible = !it.plan.empty_src && !it.plan.needs_prog && !src->host;
     for (int m = 0; m < it.plan.nmet; m++) eligible &= it.plan.wide[m] != 0;
     if (!eligible) {
       if ((st = run_star(x, b, src, refs))) return st;
@@ -2384,7 +2455,7 @@ svm_status batch_begin(Ctx* x, int n, const svm_pipeline* p, int want_host, void
       it.b = bounds[i];
       it.refs = refs;
       if ((st = plan_star_cached(x, bounds[i], src, refs, &it.plan))) return fold_fail(x, F, st);
-      bool eligible = !it.plan.empty_src && !it.plan.needs_prog;
+      bool eligible = !it.plan.empty_src && !it.plan.needs_prog && !src->host;
       for (int m = 0; m < it.plan.nmet; m++) eligible &= it.plan.wide[m] != 0;
       if (!eligible) {
         if ((st = complete_now(i))) return fold_fail(x, F, st);

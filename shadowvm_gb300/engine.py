@@ -35,6 +35,7 @@ class Engine:
         self.h = h
         self.tuple_per_bulk = tuple_per_bulk
         self.join_mode = join_mode
+        self._host_cols = {}  # host-resident objects' arrays, kept alive while the objects exist
 
     def close(self):
         if getattr(self, "h", None):
@@ -94,7 +95,26 @@ class Engine:
             return
         t = (ctypes.c_int * n)(*types)
         self._check(self.lib.svm_object_put(self.h, oid.encode(), n, t, nrows, pa, int(on_device)))
+        self._host_cols.pop(oid, None)
         del keep
+
+    def put_host(self, oid: str, columns):
+        """Store page-locked host arrays (int32/int64 numpy views of pinned
+        memory, e.g. a pinned torch tensor's .numpy()) as object `oid`, read
+        in place (svm_object_put_host).  The arrays are kept referenced until
+        the object is dropped or replaced; a None column is absent."""
+        n = len(columns)
+        lens = {len(c) for c in columns if c is not None}
+        if len(lens) > 1:
+            raise ValueError("columns differ in length")
+        nrows = lens.pop() if lens else 0
+        for c in columns:
+            if c is not None and not c.flags["C_CONTIGUOUS"]:
+                raise ValueError("host-resident columns must be contiguous")
+        types = (ctypes.c_int * n)(*[capi_type(np.int32 if c is None else c.dtype) for c in columns])
+        pa = (ctypes.c_void_p * n)(*[ctypes.c_void_p(None if c is None else c.ctypes.data) for c in columns])
+        self._check(self.lib.svm_object_put_host(self.h, oid.encode(), n, types, nrows, pa))
+        self._host_cols[oid] = list(columns)
 
     def create(self, oid: str, ncols: int, nrows: int, dtype=np.int32):
         t = (ctypes.c_int * ncols)(*([capi_type(np.dtype(dtype))] * ncols))
@@ -198,6 +218,7 @@ class Engine:
 
     def drop(self, oid: str):
         self._check(self.lib.svm_object_drop(self.h, oid.encode()))
+        self._host_cols.pop(oid, None)
 
     # ------------------------------------------------------------ pipelines
     def run(self, pipe):
