@@ -35,19 +35,20 @@ __device__ __forceinline__ void smem_add64(unsigned long long* p, unsigned long 
 // ---------------------------------------------------------------- deferred aggregation
 constexpr int kAggCap = 32;  // buffered rows per warp
 
-// A gathered value: a plain global load, since the column may be a
-// host-resident table's late column in page-locked host memory.
-__device__ __forceinline__ int32_t load_gather(const int32_t* p) {
+// A gathered value: through the read-only path from device memory, or a
+// plain global load from a host-resident table's page-locked memory.
+__device__ __forceinline__ int32_t load_gather(const int32_t* p, bool host) {
+  if (!host) return __ldg(p);
   int32_t v;
   asm("ld.global.s32 %0, [%1];" : "=r"(v) : "l"(p));
   return v;
 }
 
 // An extractor over a buffered row's words (agg_src order).
-__device__ __forceinline__ uint32_t extract_entry(const Extract& x, const uint32_t* ent) {
+__device__ __forceinline__ uint32_t extract_entry(const Extract& x, const uint32_t* ent, bool host) {
   if (x.dim < 0) return ent[x.slot] + (uint32_t)x.base;
   uint32_t v = (ent[x.dim] >> x.shift) & x.mask;
-  if (x.col) v = (uint32_t)load_gather(x.col + v);
+  if (x.col) v = (uint32_t)load_gather(x.col + v, host);
   return v + (uint32_t)x.base;
 }
 
@@ -60,11 +61,11 @@ __device__ __forceinline__ void aggregate_entry(const StarParams& P, const uint3
 #pragma unroll
   for (int m = 0; m < kMaxMetrics; m++) {
     if (m < nm) {
-      const uint32_t a = extract_entry(P.xa_e[m], ent);
+      const uint32_t a = extract_entry(P.xa_e[m], ent, P.host_late != 0);
       const int f = P.metrics[m].form;
       uint32_t v = a;
       if (f != MF_OPND) {
-        const uint32_t b = extract_entry(P.xb_e[m], ent);
+        const uint32_t b = extract_entry(P.xb_e[m], ent, P.host_late != 0);
         v = f == MF_ADD ? a + b : f == MF_SUB ? a - b : a * b;
       }
       val[m] = (int32_t)v;
@@ -83,7 +84,7 @@ __device__ __forceinline__ void aggregate_entry(const StarParams& P, const uint3
 #pragma unroll
   for (int q = 0; q < kMaxKeys; q++) {
     if (q < P.nkeys) {
-      const uint32_t off = extract_entry(P.kx_e[q], ent);
+      const uint32_t off = extract_entry(P.kx_e[q], ent, P.host_late != 0);
       in_range &= off < P.krange[q];
       gi += off * (uint32_t)P.kstride[q];
     }

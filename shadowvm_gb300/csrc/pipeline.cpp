@@ -1118,6 +1118,7 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
     if (c.rows) apply_late_columns(P);
     flatten_plan(P);
     host_unmapped = false;
+    P.host_late = src->host ? 1 : 0;
     if (src->host)
       for (int k = 0; k < P.ncols; k++) {
         auto it = host_to_dev.find(P.cols[k]);

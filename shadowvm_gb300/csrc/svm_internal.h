@@ -144,6 +144,7 @@ enum AggMode : int { AGG_SCALAR = 0, AGG_DENSE_SMEM = 1, AGG_DENSE_GLOBAL = 2, A
 struct StarParams {
   const int32_t* cols[kMaxSteps];   // fact column base pointers (row 0 of the base allocation)
   int ncols;                        // staged columns (slots 0 .. ncols-1 of cols)
+  int host_late;                    // 1: the late columns are in page-locked host memory (plain loads)
   int nlate;                        // late columns, slots ncols .. ncols+nlate-1: never staged; a
                                     // surviving row's value is read from global memory (compiled scan)
   int nstages;                      // ring depth (2..kStages)
