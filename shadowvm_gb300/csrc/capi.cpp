@@ -198,8 +198,20 @@ svm_status Ctx::column_stats(const ObjectPtr& o, int c, ColStats* out) {
     DevBufPtr d;
     svm_status st = alloc(8, &d);
     if (st) return st;
-    cudaError_t e = cudaMemcpyAsync(d->p, h, 8, cudaMemcpyHostToDevice, stream);
-    if (!e) e = launch_minmax((const int32_t*)o->col(c), o->nrows, (int32_t*)d->p, stream);
+    const int32_t* colp = (const int32_t*)o->col(c);
+    cudaError_t e = cudaSuccess;
+    if (o->host) {  // a device copy of the whole column, kept for the object's scans
+      DevBufPtr& dc = o->dev_copy[c];
+      const DevBufPtr& hb = o->storage[c];
+      if (!hb->p && o->nrows) return fail(SVM_E_INVALID_ARG, "a host-resident column the query reads has no data");
+      if (!dc) {
+        if ((st = alloc(hb->bytes + 256, &dc))) return st;
+        if (hb->bytes) e = cudaMemcpyAsync(dc->p, hb->p, hb->bytes, cudaMemcpyHostToDevice, stream);
+      }
+      colp = (const int32_t*)dc->p + o->row0;
+    }
+    if (!e) e = cudaMemcpyAsync(d->p, h, 8, cudaMemcpyHostToDevice, stream);
+    if (!e) e = launch_minmax(colp, o->nrows, (int32_t*)d->p, stream);
     if (!e) e = cudaMemcpyAsync(h, d->p, 8, cudaMemcpyDeviceToHost, stream);
     if (!e) e = cudaStreamSynchronize(stream);
     if (e) return cuda_fail(e, "column statistics");

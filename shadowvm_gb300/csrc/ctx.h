@@ -74,6 +74,10 @@ struct Object {
   // object (as its fact table), copying the columns its filters read and
   // gathering the others at the surviving rows.
   bool host = false;
+  // A host-resident object's whole-column device copies, made when a column's
+  // statistics are needed (its values cross the host link once); a scan of
+  // the object reuses them instead of copying those rows again.
+  std::map<int, DevBufPtr> dev_copy;
   // The reference keeps objects as bulks of tuple_per_bulk rows and joins only
   // against bulk 0 of a joined object (core/pipeline.cu:91,295).
   bool has_bulks = false;

@@ -1199,9 +1199,18 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
       const int32_t* h = P.cols[k];
       if (host_to_dev.count(h)) continue;
       const DevBuf* hb = nullptr;
-      for (const DevBufPtr& s : src->storage)
-        if (s && s->p == (const void*)h) hb = s.get();
+      int hk = -1;
+      for (size_t s = 0; s < src->storage.size(); s++)
+        if (src->storage[s] && src->storage[s]->p == (const void*)h) {
+          hb = src->storage[s].get();
+          hk = (int)s;
+        }
       if (!h || !hb) return x->fail(SVM_E_INVALID_ARG, "a host-resident column the scan reads has no data");
+      auto dc = src->dev_copy.find(hk);
+      if (dc != src->dev_copy.end() && dc->second) {  // copied already, for its statistics
+        host_to_dev[h] = (const int32_t*)dc->second->p;
+        continue;
+      }
       const long long base_rows = (long long)(hb->bytes / 4);
       const long long hi = std::min(end4, base_rows);
       DevBufPtr d;
