@@ -119,3 +119,33 @@ def test_host_resident_object_refusals(engine_factory):
     assert "INVALID_ARG" in str(ei.value), ei.value
     eng.drop("lineorder_h")
     del keep
+
+
+@pytest.mark.parametrize("config", [0, 2])
+def test_host_resident_ragged_row_count(engine_factory, config):
+    """A row count that is no multiple of 4 (the scan's last 16-byte reads run
+    past the host column's end, whose rows the copy must not read) and a view
+    that ends on the table's last row: the same rows as on the device."""
+    kw = dict(fact_rows=123_457, tuple_per_bulk=100_000)
+    if config == 2:
+        kw.update(n_part=20_000, n_cust=30_000, n_supp=5_000)
+    w = W.make(config, **kw)
+    eng = engine_factory(tuple_per_bulk=w.tuple_per_bulk)
+    W.load_engine(eng, w)
+    dk, ds = W.run_engine(eng, w)
+    cols, keep = pinned_copy(eng, "lineorder", len(w.fact_cols))
+    eng.put_host("lineorder_h", cols)
+    q = on(w.query, "lineorder_h")
+    eng.run(q)
+    hk, hs = eng.result(q.id, w.key_num)
+    np.testing.assert_array_equal(hk, dk)
+    np.testing.assert_array_equal(hs, ds)
+    eng.view("lineorder_hv", "lineorder_h", 5, w.fact_rows - 5)
+    eng.view("lineorder_dv", "lineorder", 5, w.fact_rows - 5)
+    qv, qd = on(w.query, "lineorder_hv"), on(w.query, "lineorder_dv")
+    eng.run(qv)
+    eng.run(qd)
+    np.testing.assert_array_equal(eng.result(qv.id, w.key_num)[1], eng.result(qd.id, w.key_num)[1])
+    eng.drop("lineorder_hv")
+    eng.drop("lineorder_h")
+    del keep
