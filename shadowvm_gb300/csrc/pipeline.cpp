@@ -1249,6 +1249,11 @@ svm_status run_star(Ctx* x, const Bound& b, const ObjectPtr& src, const std::vec
       float best = 0.f;
       for (const Fit& f : cands) {
         configure(f.c);
+        // Candidates are ranked on the first kTuneRows rows of the scan (the
+        // query itself then runs whole with the pick), so that the first run
+        // of a shape costs tens of milliseconds, not a full scan per candidate.
+        constexpr long long kTuneRows = 1ll << 25;
+        if (P.row_end - P.row_begin > kTuneRows) P.row_end = P.row_begin + kTuneRows;
         const size_t sm = smem_of(f.c);
         if (!e) e = cudaMemsetAsync(sums, 0, agg_bytes, x->stream);
         if (!e) e = cudaEventRecord(t0, x->stream);
