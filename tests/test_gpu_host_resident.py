@@ -149,3 +149,29 @@ def test_host_resident_ragged_row_count(engine_factory, config):
     eng.drop("lineorder_hv")
     eng.drop("lineorder_h")
     del keep
+
+
+def test_host_resident_query_in_a_fold(engine_factory):
+    """A fold in flight (svm_batch_begin) with a query over a host-resident
+    table runs that query alone inside the call; its result and the batched
+    one over the device table both equal the queries run alone."""
+    from shadowvm_gb300.serving import sink_types
+    case = GOLDEN["c2_small"]
+    w = W.make(case["config"], **case["kwargs"])
+    eng = engine_factory(tuple_per_bulk=w.tuple_per_bulk, batch_policy="always")
+    W.load_engine(eng, w)
+    dk, ds = W.run_engine(eng, w)
+    cols, keep = pinned_copy(eng, "lineorder", len(w.fact_cols))
+    eng.put_host("lineorder_h", cols)
+    q_h, q_d = on(w.query, "lineorder_h"), on(w.query, "lineorder")
+    f = eng.batch_begin([q_h, q_d], host_results=True)
+    rows = f.wait()
+    f.release([sink_types(p) for p in (q_h, q_d)])
+    for q in (q_h, q_d):
+        k, v = eng.result(q.id, w.key_num)
+        np.testing.assert_array_equal(k, dk)
+        np.testing.assert_array_equal(v, ds)
+    assert rows == [len(ds), len(ds)]
+    eng.drop("lineorder_h")
+    del keep
+

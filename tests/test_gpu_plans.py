@@ -118,6 +118,9 @@ def test_star_join_list_form_keeps_three_blocks_per_sm(engine_factory):
     launch = eng.last_launch()
     assert launch["kernel"] == "compiled plan" and launch["list_after_step"] == 0, launch
     assert launch["blocks_per_sm"] >= 3, launch
+    for bad in (-2, 5):  # list_after is -1 (any), 0..2, 3 (none) or 4
+        with pytest.raises(SvmError):
+            eng.pin_list_after(bad)
     eng.close()
 
 
