@@ -1571,6 +1571,7 @@ struct MergePlan {
   struct Share {
     int word = 0, bit = 0, bits = 0;  // bits 0: the group has no shared field
     int32_t base = 0;                 // field = value - base
+    bool relative = false;            // field = value - the table's own payload minimum (base unused)
   };
   std::map<std::pair<int, const DimTable*>, Place> place;  // (union column, table) -> placement
   std::vector<ProbeGroup> groups;
@@ -1603,15 +1604,23 @@ void plan_merge(Ctx* x, const std::vector<BatchQuery>& qs, const std::vector<Bat
       return d.npay == 1 && d.pay[0].col == nullptr && d.pay[0].bits > 0 && T->live > 0 && !x->share_refused(T);
     };
     long long smin = LLONG_MAX, smax = LLONG_MIN;
-    int nshare = 0, own_bits = 0;
+    int nshare = 0, own_bits = 0, rbits = 0;
     for (const DimTablePtr& T : tabs)
       if (sharable(T)) {
         nshare++;
         own_bits += T->desc.pay[0].bits;
+        rbits = std::max(rbits, (int)T->desc.pay[0].bits);
         smin = std::min<long long>(smin, T->pay_min[0]);
         smax = std::max<long long>(smax, T->pay_max[0]);
       }
-    const int sbits = nshare >= 2 ? ceil_log2((unsigned long long)(smax - smin + 1)) : 0;
+    // The shared field holds value - the tables' common minimum (absolute),
+    // or, when narrower, value - each table's own minimum (relative: as wide
+    // as the widest table's own range; a key two tables hold must then have
+    // the same relative value in both, which the build checks like the
+    // absolute field's agreement).
+    const int abits = nshare >= 2 ? ceil_log2((unsigned long long)(smax - smin + 1)) : 0;
+    const bool relative = nshare >= 2 && rbits < abits;
+    const int sbits = relative ? rbits : abits;
     const bool share = nshare >= 2 && sbits < own_bits && sbits <= 31;
     size_t next = 0;
     while (next < tabs.size() && (int)mp->groups.size() < kMaxProbeGroups) {
@@ -1662,7 +1671,7 @@ void plan_merge(Ctx* x, const std::vector<BatchQuery>& qs, const std::vector<Bat
             pl.pay_bit = 32 - freebits[word - 1];
             freebits[word - 1] -= pb;
           }
-          if (shared) sh = MergePlan::Share{word, pl.pay_bit, sbits, (int32_t)smin};
+          if (shared) sh = MergePlan::Share{word, pl.pay_bit, sbits, relative ? 0 : (int32_t)smin, relative};
         }
         if (shared) {
           pl.shared = true;
@@ -1724,7 +1733,7 @@ svm_status merged_table(Ctx* x, MergePlan* mp, int g, unsigned int* conflict, st
   for (auto& m : mp->members[g]) {
     key += "|" + std::to_string((uintptr_t)m.first.get()) + "@" + std::to_string(m.second.present_bit) + "." +
            std::to_string(m.second.pay_word) + "." + std::to_string(m.second.pay_bit);
-    if (m.second.shared) key += "s" + std::to_string(sh.bits) + "." + std::to_string(sh.base);
+    if (m.second.shared) key += "s" + std::to_string(sh.bits) + "." + std::to_string(sh.base) + (sh.relative ? "r" : "");
   }
   checked->clear();
   auto it = x->merged_cache.find(key);
@@ -1750,7 +1759,8 @@ svm_status merged_table(Ctx* x, MergePlan* mp, int g, unsigned int* conflict, st
         const DimDesc& d = m.first->desc;
         int pb = 0;
         for (int f = 0; f < d.npay; f++) pb = std::max(pb, (int)d.pay[f].shift + (int)d.pay[f].bits - 1);
-        const int32_t off = m.second.shared ? (int32_t)((uint32_t)d.pay[0].min - (uint32_t)sh.base) : 0;
+        const int32_t off =
+            m.second.shared && !sh.relative ? (int32_t)((uint32_t)d.pay[0].min - (uint32_t)sh.base) : 0;
         mb.src[mb.nsrc++] = MergeSrc{d.words,          d.key_min,          d.span, d.entry_bits,
                                      m.second.present_bit, m.second.pay_word, m.second.pay_bit, pb,
                                      m.second.shared ? 1 : 0, off};
@@ -1967,12 +1977,12 @@ svm_status exec_batch(Ctx* x, std::vector<BatchItem>& items, FoldPart* async_par
         r.slot = (uint8_t)pl.pay_word;
         r.sg = (uint8_t)mp.groups[pl.group].words;
         r.shift = (uint8_t)(pl.pay_bit + (e.mask ? e.shift - 1 : 0));
-        if (pl.shared && e.mask) {  // the group's shared field holds value - sh.base
+        if (pl.shared && e.mask) {  // the group's shared field holds value - sh.base (or - the table's minimum)
           const MergePlan::Share& sh = mp.share[pl.group];
           const DimDesc& d = items[i].plan.dim_tables[e.dim]->desc;
           r.shift = (uint8_t)sh.bit;
           r.mask = sh.bits >= 32 ? 0xFFFFFFFFu : (1u << sh.bits) - 1u;
-          r.base = (int32_t)((uint32_t)e.base - (uint32_t)d.pay[0].min + (uint32_t)sh.base);
+          if (!sh.relative) r.base = (int32_t)((uint32_t)e.base - (uint32_t)d.pay[0].min + (uint32_t)sh.base);
         }
         if (e.col) {
           size_t gi = std::find(gcols.begin(), gcols.end(), e.col) - gcols.begin();
