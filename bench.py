@@ -517,6 +517,9 @@ def batched_arm(args):
     bw = W.make_batch(256, fact_rows=args.rows)
     rows = bw.fact.fact_rows
     eng = Engine(device=local, tuple_per_bulk=bw.fact.tuple_per_bulk, join_mode=args.join_mode)
+    if args.pin_batch:
+        cw, st = (int(v) for v in args.pin_batch.split(","))
+        eng.pin_batch_launch(cw, st)
     W.load_engine(eng, bw.fact, row0=rank * rows)
     for i, q in enumerate(bw.queries):
         eng.view(f"lo_q{i}", "lineorder", q.row0, q.nrows)
@@ -768,6 +771,9 @@ def main():
     ap.add_argument("--max-fold", type=int, default=1024, help="config 4: most requests in one fold")
     ap.add_argument("--inflight", type=int, default=2, help="config 4: folds begun and not complete, at most")
     ap.add_argument("--loader", action="store_true", help="measure the text Loader instead")
+    ap.add_argument("--pin-batch", default=None,
+                    help="consumer_warps,ring_stages: pin the merged batch kernel's launch configuration "
+                         "(svm_pin_batch_launch), e.g. for a profile of the tuned variant")
     ap.add_argument("--pin", default=None,
                     help="rows_per_lane,blocks_per_sm,ring_stages,tables_staged[,list_after]: pin the scan's "
                          "launch configuration (svm_pin_launch, svm_pin_list_after), e.g. for a profile of "
